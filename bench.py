@@ -1,0 +1,317 @@
+"""Benchmark: Fletcher TTI FP32 propagation at 504^3 interior on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (one "step" = one propagation step of the whole grid): the layered
+504^3-interior model (576^3 grid, bord 4, absorb 32, dt 0.6 ms, 15 Hz Ricker
+at (288, 288, 44)), synthetic and seeded.  The line printed by rank 0:
+
+  value     MSamples/s by the reference's definition (original/model.c:44,117:
+            updated cells x steps / time), K steps timed with CUDA events on the
+            library's stream, inputs resident in HBM (11+ GB, larger than L2,
+            so no flush is needed between steps);
+  e2e       the same metric through the C ABI with host buffers: the
+            reference's Model() sequence (FLETCHER_Model: DRIVER_Initialize with
+            the host-to-device copy of the model and fields, per step
+            InsertSource + Propagate, a device-to-host snapshot of p every
+            0.01 s of simulated time, final read-back), wall-clock;
+  roofline  the propagate kernel against the measured HBM copy bandwidth;
+            algorithmic bytes = 64 B per updated cell (fields 16 B read + 8 B
+            written, ten coefficients 40 B);
+  cpu_baseline  the oracle (the reference's FP32 OpenMP loop restated) on
+            this machine's host cores, on a bounded sample (a 16-plane slab).
+
+N > 1: replicas only -- every rank runs the whole workload on its own GPU,
+no data exchange; timing is the max over ranks, value the sum of cells/time.
+`--impl reference` times the reference's CPU algorithm (the oracle port) on
+the host cores: each step is one propagation of a 16-plane slab of the same
+grid (a bounded sample of the workload).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MSamples/s + HBM GB/s at 504^3: FP32 vs FP16-store/learned-ABC, equal L2 err"
+UNIT = "MSamples/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Group:
+    """Host-side coordination of replicas (gloo): barrier and max/sum of scalars."""
+
+    def __init__(self, ws: int):
+        self.ws = ws
+        if ws > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def reduce(self, x: float, op: str) -> float:
+        if self.ws == 1:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX if op == "max" else self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic_per_cell():
+    """DRAM bytes per updated cell of the propagate kernel from the committed
+    ncu summary (profiles/propagate_fp32_traffic.json), or None."""
+    path = os.path.join(ROOT, "profiles", "propagate_fp32_traffic.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["dram_bytes_per_cell"])
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(s):
+            try:
+                return float(s)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
+
+
+def run_gb300(args, ws, rank, local, group):
+    import torch
+
+    from fletcher_petrobras_gb300 import C1, Propagator
+    from fletcher_petrobras_gb300._lib import fptr, load
+
+    torch.cuda.set_device(local)
+    lib = load()
+    prob = C1
+    K, W = args.steps, args.warmup
+    model = prob.model()
+    src = prob.sources(W + K)
+    stream = torch.cuda.Stream()
+    prop = Propagator(stream=stream.cuda_stream)
+    prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model)
+    prop.run(W, prob.i_source, src[:W])
+    prop.synchronize()
+    launches0 = prop.kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    group.barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    prop.run(K, prob.i_source, src[W:W + K])
+    ev1.record(stream)
+    prop.synchronize()
+    torch.cuda.synchronize()
+    group.barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    launches = prop.kernel_launches() - launches0
+    bpc = prop.bytes_per_cell()
+    dev_gb = prop.device_bytes() / 1e9
+    prop.finalize()
+
+    ms_max = group.reduce(ms, "max")
+    cells = prob.updated_cells
+    value = ws * cells * K / (ms_max / 1e3) / 1e6  # all ranks' cells over the slowest rank's time
+    per_launch_s = ms / 1e3 / K
+    achieved = bpc * cells / per_launch_s / 1e9
+    peak, peak_kind = measured_peak()
+    tpc = ncu_traffic_per_cell()
+
+    # End to end through the C ABI with host buffers (the reference's Model() sequence).
+    import ctypes as C
+
+    n = prob.n
+    f = np.zeros((4, n), np.float32)
+    stats = (C.c_double * 5)()
+    group.barrier()
+    rc = lib.FLETCHER_Model(K, prob.i_source, prob.fcut, 0.01, prob.sx, prob.sy, prob.sz, prob.bord, prob.dx,
+                            prob.dy, prob.dz, prob.dt, *[fptr(f[k]) for k in range(4)],
+                            *[fptr(model[k]) for k in range(6)], stats)
+    if rc:
+        raise RuntimeError("FLETCHER_Model failed: " + lib.FLETCHER_GetLastErrorString().decode())
+    e2e_wall = group.reduce(stats[2], "max")
+    e2e = ws * cells * K / e2e_wall / 1e6
+    del f
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        import oracle
+
+        r = oracle.time_slab(prob, model, nplanes=16, min_seconds=args.cpu_seconds)
+        cpu = {"value": round(r["msamples"], 2), "unit": UNIT, "cores": r["threads"], "kind": "port",
+               "sample": f"{r['steps']} FP32 steps of a {r['planes']}-plane slab of the 576^3 grid "
+                         f"({r['cells']} updated cells/step, {r['seconds']:.1f} s), oracle restatement of "
+                         "original/OpenMP/openmp_propagate.c + original/sample.h, gcc -O3 -fopenmp"}
+    group.barrier()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+        "ms_per_step": round(ms_max / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded 8-layer TTI model, random-velocity boundary)",
+        "config": {"workload": "C1: plain FP32 single shot, 504^3 interior (576^3 grid), bord 4, absorb 32, "
+                               "dx 12.5 m, dt 0.6 ms, 8-layer seeded TTI, 15 Hz Ricker at (288,288,44)",
+                   "grid": [prob.sx, prob.sy, prob.sz], "updated_cells_per_step": cells,
+                   "form": "fp32", "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": f"inputs resident in HBM ({dev_gb:.1f} GB) are larger than L2 (129 MB); no flush",
+                   "timed_steps_include": "fused source injection + one propagate launch per step"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "algorithmic_bytes_per_cell": bpc,
+                     "traffic": None if tpc is None else round(tpc * cells / 1e9, 3),
+                     "traffic_unit": "GB per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+                     "kernel": "k_propagate_fp32"},
+        "e2e": {"value": round(e2e, 1), "unit": UNIT, "h2d_bytes_per_step": int(stats[3] / K),
+                "d2h_bytes_per_step": int(stats[4] / K), "wall_s": round(e2e_wall, 3),
+                "what": "FLETCHER_Model via the C ABI: DRIVER_Initialize (H2D of 6 model + 4 field arrays, "
+                        "FP64 coefficient precompute) + K x (InsertSource, Propagate) + D2H snapshot of p every "
+                        "0.01 s simulated + final D2H of p,q"},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def run_reference(args, ws, rank, group):
+    """The reference's CPU algorithm (its FP32 OpenMP loop, restated by the
+    oracle) on the host cores, each step one propagation of a 16-plane slab
+    of the same 576^3 grid."""
+    if rank != 0:
+        return
+    import oracle
+    from fletcher_petrobras_gb300 import C1
+
+    prob = C1
+    model = prob.model()
+    K, W = args.steps, args.warmup
+    if W:
+        oracle.time_slab(prob, model, nplanes=16, steps=W)
+    r = oracle.time_slab(prob, model, nplanes=16, steps=K)
+    v = round(r["msamples"], 2)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+        "ms_per_step": round(1e3 * r["seconds"] / K, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded 8-layer TTI model)",
+        "config": {"workload": "C1: plain FP32 single shot, 504^3 interior (576^3 grid); each step is one "
+                               f"propagation of a {r['planes']}-plane slab ({r['cells']} cells)",
+                   "grid": [prob.sx, prob.sy, prob.sz]},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": r["threads"], "kind": "port",
+                         "sample": f"{K} steps of a {r['planes']}-plane slab of the 576^3 grid"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    ws, rank, local = dist_env()
+    group = Group(ws)
+    try:
+        if args.impl == "reference":
+            run_reference(args, ws, rank, group)
+        else:
+            run_gb300(args, ws, rank, local, group)
+    finally:
+        group.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,72 @@
+"""ctypes binding of libfletcher_gb300.so (include/fletcher_gb300.h)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from .build import LIB as _LIB_PATH, build as _do_build
+
+_LIB = None
+
+FP = C.POINTER(C.c_float)
+DP = C.POINTER(C.c_double)
+IP = C.POINTER(C.c_int)
+
+# name -> (restype, argtypes); every symbol declared in include/fletcher_gb300.h.
+SIGNATURES = {
+    "DRIVER_Initialize": (None, [C.c_int] * 4 + [C.c_float] * 4 + [FP] * 10),
+    "DRIVER_Finalize": (None, []),
+    "DRIVER_Propagate": (None, [C.c_int] * 4 + [C.c_float] * 4 + [C.c_int] + [FP] * 4),
+    "DRIVER_Update_pointers": (None, [C.c_int] * 3 + [FP]),
+    "DRIVER_InsertSource": (None, [C.c_float, C.c_int, C.c_int, FP, FP, C.c_float]),
+    "FLETCHER_SetErrorMode": (None, [C.c_int]),
+    "FLETCHER_GetLastError": (C.c_int, []),
+    "FLETCHER_GetLastErrorString": (C.c_char_p, []),
+    "FLETCHER_ClearError": (None, []),
+    "FLETCHER_SetStream": (C.c_int, [C.c_void_p]),
+    "FLETCHER_GetStream": (C.c_void_p, []),
+    "FLETCHER_SetForm": (C.c_int, [C.c_int]),
+    "FLETCHER_SetTileConfig": (C.c_int, [C.c_int, C.c_int, C.c_int]),
+    "FLETCHER_Run": (C.c_int, [C.c_int, C.c_long, FP]),
+    "FLETCHER_Synchronize": (C.c_int, []),
+    "FLETCHER_GetField": (C.c_int, [C.c_int, FP]),
+    "FLETCHER_GetCoefficients": (C.c_int, [FP]),
+    "FLETCHER_KernelLaunches": (C.c_long, []),
+    "FLETCHER_DeviceBytes": (C.c_size_t, []),
+    "FLETCHER_BytesPerCell": (C.c_double, []),
+    "FLETCHER_ModelHomogeneous": (None, [C.c_long] + [C.c_float] * 6 + [FP]),
+    "FLETCHER_ModelLayered": (None, [C.c_int] * 6 + [C.c_uint64] + [C.c_float] * 3 + [FP, IP]),
+    "FLETCHER_RandomVelocityBoundary": (None, [C.c_int] * 8 + [FP, FP, C.c_uint]),
+    "FLETCHER_Source": (C.c_float, [C.c_float, C.c_int, C.c_double]),
+    "FLETCHER_RecommendedDt": (C.c_float, [C.c_long, FP, FP, C.c_float, C.c_float, C.c_float]),
+    "FLETCHER_Model": (C.c_int, [C.c_int, C.c_long, C.c_double, C.c_float] + [C.c_int] * 4 + [C.c_float] * 4
+                       + [FP] * 10 + [DP]),
+}
+
+
+def lib_path() -> str:
+    return _LIB_PATH
+
+
+def load(build_if_missing: bool = True):
+    """Loads the library; fails loudly when it is missing and cannot be built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"libfletcher_gb300.so not built ({path}); run fletcher_petrobras_gb300.build")
+        _do_build()
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    lib.FLETCHER_SetErrorMode(1)  # record and return: the Python layer raises
+    _LIB = lib
+    return lib
+
+
+def fptr(a):
+    return a.ctypes.data_as(FP) if a is not None else None

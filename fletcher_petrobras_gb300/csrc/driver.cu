@@ -1,0 +1,582 @@
+// C-ABI layer of libfletcher_gb300.so: the reference back-end interface
+// (original/driver.h:8-22) and the extension entry points declared in
+// include/fletcher_gb300.h, over resident device state.
+//
+// Device layout (single GPU, everything resident in HBM):
+//   F[0], F[1]  (p, q) pairs of float, [sz][sy][pitch], pitch = sx rounded
+//               up to 32; one buffer holds the current field, the other the
+//               previous field, and they swap after every step;
+//   coef        ten FP32 coefficient fields, [sz][10][sy][pitch], computed on
+//               the GPU in FP64 from the raw model arrays;
+//   scratch     one unpitched sx*sy*sz float volume for host transfers.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../../include/fletcher_gb300.h"
+#include "fletcher_internal.h"
+
+using namespace flt;
+
+namespace {
+
+struct Source {
+  bool on = false;
+  long idx = 0;
+  float val = 0.f;
+};
+
+struct State {
+  bool init = false;
+  int sx = 0, sy = 0, sz = 0, bord = 0, pitch = 0;
+  float dx = 0, dy = 0, dz = 0, dt = 0;
+  size_t n = 0;        // sx*sy*sz
+  size_t npitch = 0;   // pitch*sy*sz
+  float2 *F[2] = {nullptr, nullptr};
+  float *coef = nullptr;
+  float *scratch = nullptr;
+  unsigned *err_host = nullptr, *err_dev = nullptr;
+  int cur = 0;
+  Source pending;      // registered by DRIVER_InsertSource, applied by the next step
+  Source owed;         // source of the last step, missing from the previous-field buffer
+  CUtensorMap halo[2], pt[2], arr, upd;
+  int tile_rows = 12, stages = 4, zchunks = 0;
+  int grid = 0, nitems = 0, ntx = 0, nty = 0, nchunk = 0, chunk = 0;
+  long launches = 0;
+  size_t dev_bytes = 0;
+  int num_sms = 0;
+};
+
+State g;
+cudaStream_t g_stream = nullptr;
+bool g_own_stream = false;
+int g_form = FLETCHER_FORM_FP32;
+int g_req_rows = 0, g_req_stages = 0, g_req_chunks = 0;
+int g_errmode = FLETCHER_ERRMODE_EXIT;
+int g_last_err = FLETCHER_OK;
+char g_errmsg[512] = "";
+
+int fail(int code, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_errmsg, sizeof(g_errmsg), fmt, ap);
+  va_end(ap);
+  fprintf(stderr, "fletcher_gb300: %s\n", g_errmsg);
+  if (g_last_err == FLETCHER_OK) g_last_err = code;
+  if (g_errmode == FLETCHER_ERRMODE_EXIT) exit(1);
+  return code;
+}
+
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess)                                                                         \
+      return fail(e_ == cudaErrorMemoryAllocation ? FLETCHER_ERR_NOMEM : FLETCHER_ERR_CUDA,       \
+                  "%s failed at %s:%d: %s", #call, __FILE__, __LINE__, cudaGetErrorString(e_));   \
+  } while (0)
+
+// ---- auxiliary kernels --------------------------------------------------------
+
+// Coefficient precompute, original/precomp.h:14-38 and :49-58: trigonometry
+// in FP64 rounded to float, products of those floats in float, velocity
+// terms in FP64.  raw = vpz vsv epsilon delta phi theta (n floats each).
+__global__ void k_precompute(const float *__restrict__ raw, float *__restrict__ coef, int sx, int sy, int sz,
+                             int pitch) {
+  const size_t n = (size_t)sx * sy * sz;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float vpz = raw[i], vsv = raw[n + i], eps = raw[2 * n + i], del = raw[3 * n + i];
+    const float phi = raw[4 * n + i], theta = raw[5 * n + i];
+    const float sinTheta = (float)sin((double)theta);
+    const float cosTheta = (float)cos((double)theta);
+    const float sin2Theta = (float)sin(__dmul_rn(2.0, (double)theta));
+    const float sinPhi = (float)sin((double)phi);
+    const float cosPhi = (float)cos((double)phi);
+    const float sin2Phi = (float)sin(__dmul_rn(2.0, (double)phi));
+    const float v2sz = __fmul_rn(vsv, vsv);
+    const float v2pz = __fmul_rn(vpz, vpz);
+    const float v2px = (float)__dmul_rn((double)v2pz, __dadd_rn(1.0, __dmul_rn(2.0, (double)eps)));
+    const float v2pn = (float)__dmul_rn((double)v2pz, __dadd_rn(1.0, __dmul_rn(2.0, (double)del)));
+    float c[kNumCoef];
+    c[DC_XX] = __fmul_rn(__fmul_rn(__fmul_rn(sinTheta, sinTheta), cosPhi), cosPhi);
+    c[DC_YY] = __fmul_rn(__fmul_rn(__fmul_rn(sinTheta, sinTheta), sinPhi), sinPhi);
+    c[DC_XY] = __fmul_rn(__fmul_rn(sinTheta, sinTheta), sin2Phi);
+    c[DC_ZZ] = __fmul_rn(cosTheta, cosTheta);
+    c[DC_XZ] = __fmul_rn(sin2Theta, cosPhi);
+    c[DC_YZ] = __fmul_rn(sin2Theta, sinPhi);
+    c[DC_V2PX] = v2px;
+    c[DC_V2PZ] = v2pz;
+    c[DC_V2SZ] = v2sz;
+    c[DC_V2PN] = v2pn;
+    const size_t x = i % sx, y = (i / sx) % sy, z = i / ((size_t)sx * sy);
+#pragma unroll
+    for (int k = 0; k < kNumCoef; ++k) coef[((z * kNumCoef + k) * sy + y) * pitch + x] = c[k];
+  }
+}
+
+// (p, q) volumes -> pitched pair buffer.  Null p or q gives zeros.
+__global__ void k_pack(const float *__restrict__ p, const float *__restrict__ q, float2 *__restrict__ F, int sx,
+                       int sy, int sz, int pitch) {
+  const size_t n = (size_t)sx * sy * sz;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t x = i % sx, yz = i / sx;
+    F[yz * pitch + x] = make_float2(p ? p[i] : 0.f, q ? q[i] : 0.f);
+  }
+}
+
+// One component of a pitched pair buffer -> unpitched volume.
+__global__ void k_unpack(const float2 *__restrict__ F, float *__restrict__ out, int comp, int sx, int sy, int sz,
+                         int pitch) {
+  const size_t n = (size_t)sx * sy * sz;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t x = i % sx, yz = i / sx;
+    const float2 v = F[yz * pitch + x];
+    out[i] = comp ? v.y : v.x;
+  }
+}
+
+// Coefficient k of the device block -> unpitched volume.
+__global__ void k_unpack_coef(const float *__restrict__ coef, float *__restrict__ out, int k, int sx, int sy, int sz,
+                              int pitch) {
+  const size_t n = (size_t)sx * sy * sz;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t x = i % sx, y = (i / sx) % sy, z = i / ((size_t)sx * sy);
+    out[i] = coef[((z * kNumCoef + k) * sy + y) * pitch + x];
+  }
+}
+
+// Adds val to both fields of one cell (source outside the fused path).
+__global__ void k_add_source(float2 *F, size_t idx, float val) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    float2 v = F[idx];
+    v.x = v.x + val;
+    v.y = v.y + val;
+    F[idx] = v;
+  }
+}
+
+// ---- helpers -------------------------------------------------------------------
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+int encode(CUtensorMap *m, CUtensorMapDataType dt, int rank, void *base, const cuuint64_t *dims,
+           const cuuint64_t *strides, const cuuint32_t *box) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return fail(FLETCHER_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  CUresult r = fn(m, dt, (cuuint32_t)rank, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(FLETCHER_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return FLETCHER_OK;
+}
+
+int grid_for(size_t n) {
+  size_t b = (n + 255) / 256;
+  const size_t cap = (size_t)(g.num_sms > 0 ? g.num_sms : 148) * 16;
+  return (int)(b < cap ? (b ? b : 1) : cap);
+}
+
+// Chooses the number of z-chunks: balances the persistent CTAs' last round
+// against the 8 warm-up planes each chunk re-reads.
+void choose_chunks(int ctas, int tiles, int depth, int req, int *nchunk, int *chunk) {
+  if (req > 0) {
+    *nchunk = req < depth ? req : depth;
+  } else {
+    double best = -1.0;
+    int bc = 1;
+    for (int c = 1; c <= 16 && c <= depth; ++c) {
+      const int len = (depth + c - 1) / c;
+      const int cc = (depth + len - 1) / len;
+      const double items = (double)tiles * cc;
+      const double rounds = ceil(items / ctas);
+      const double eff = (items / ctas) / rounds * (double)len / (len + 4.0);
+      if (eff > best + 1e-9) {
+        best = eff;
+        bc = c;
+      }
+    }
+    *nchunk = bc;
+  }
+  *chunk = (depth + *nchunk - 1) / *nchunk;
+  *nchunk = (depth + *chunk - 1) / *chunk;
+}
+
+int check_dims(int sx, int sy, int sz) {
+  if (!g.init) return fail(FLETCHER_ERR_ARGS, "DRIVER_Initialize has not been called");
+  if (sx != g.sx || sy != g.sy || sz != g.sz)
+    return fail(FLETCHER_ERR_ARGS, "grid %dx%dx%d differs from the initialised %dx%dx%d", sx, sy, sz, g.sx, g.sy,
+                g.sz);
+  return FLETCHER_OK;
+}
+
+size_t pitched_index(long idx) {
+  const long x = idx % g.sx, yz = idx / g.sx;
+  return (size_t)yz * g.pitch + x;
+}
+
+bool in_update_region(long idx) {
+  const long x = idx % g.sx, y = (idx / g.sx) % g.sy, z = idx / ((long)g.sx * g.sy);
+  return x >= g.bord && x < g.sx - g.bord && y >= g.bord && y < g.sy - g.bord && z >= g.bord && z < g.sz - g.bord;
+}
+
+int check_err_word() {
+  if (g.err_host && *(volatile unsigned *)g.err_host)
+    return fail(FLETCHER_ERR_TIMEOUT, "a propagate kernel gave up waiting for its data (error word 0x%x)",
+                *(volatile unsigned *)g.err_host);
+  return FLETCHER_OK;
+}
+
+void free_state() {
+  if (g.F[0]) cudaFree(g.F[0]);
+  if (g.F[1]) cudaFree(g.F[1]);
+  if (g.coef) cudaFree(g.coef);
+  if (g.scratch) cudaFree(g.scratch);
+  if (g.err_host) cudaFreeHost(g.err_host);
+  g = State();
+}
+
+int ensure_stream() {
+  if (!g_stream) {
+    CK(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+    g_own_stream = true;
+  }
+  return FLETCHER_OK;
+}
+
+int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, float dt, const float *vpz,
+               const float *vsv, const float *epsilon, const float *delta, const float *phi, const float *theta,
+               const float *pp, const float *pc, const float *qp, const float *qc) {
+  if (g.init) free_state();
+  if (bord < kRadius) return fail(FLETCHER_ERR_ARGS, "bord (%d) must be at least the stencil radius %d", bord, kRadius);
+  if (sx <= 2 * bord || sy <= 2 * bord || sz <= 2 * bord)
+    return fail(FLETCHER_ERR_ARGS, "grid %dx%dx%d has no interior for bord %d", sx, sy, sz, bord);
+  if (!(dx > 0.f) || !(dy > 0.f) || !(dz > 0.f)) return fail(FLETCHER_ERR_ARGS, "grid spacing must be positive");
+  if (!vpz || !vsv || !epsilon || !delta || !phi || !theta)
+    return fail(FLETCHER_ERR_ARGS, "model arrays must not be NULL");
+  if (g_form != FLETCHER_FORM_FP32) return fail(FLETCHER_ERR_ARGS, "unknown storage form %d", g_form);
+  const int rows = g_req_rows ? g_req_rows : 12;
+  const int stages = g_req_stages ? g_req_stages : 4;
+  if (!propagate_fp32_supported(rows, stages))
+    return fail(FLETCHER_ERR_ARGS, "tile shape (%d rows, %d stages) is not built", rows, stages);
+  if (ensure_stream()) return g_last_err;
+
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&g.num_sms, cudaDevAttrMultiProcessorCount, dev));
+  g.sx = sx; g.sy = sy; g.sz = sz; g.bord = bord;
+  g.dx = dx; g.dy = dy; g.dz = dz; g.dt = dt;
+  g.pitch = (sx + 31) / 32 * 32;
+  g.n = (size_t)sx * sy * sz;
+  g.npitch = (size_t)g.pitch * sy * sz;
+  g.tile_rows = rows;
+  g.stages = stages;
+  g.zchunks = g_req_chunks;
+  cudaStream_t s = g_stream;
+
+  CK(cudaMalloc(&g.F[0], g.npitch * sizeof(float2)));
+  CK(cudaMalloc(&g.F[1], g.npitch * sizeof(float2)));
+  CK(cudaMalloc(&g.coef, g.npitch * kNumCoef * sizeof(float)));
+  CK(cudaMalloc(&g.scratch, g.n * sizeof(float)));
+  CK(cudaHostAlloc(&g.err_host, sizeof(unsigned), cudaHostAllocMapped));
+  *g.err_host = 0;
+  CK(cudaHostGetDevicePointer((void **)&g.err_dev, g.err_host, 0));
+  g.dev_bytes = 2 * g.npitch * sizeof(float2) + g.npitch * kNumCoef * sizeof(float) + g.n * sizeof(float);
+  CK(cudaMemsetAsync(g.F[0], 0, g.npitch * sizeof(float2), s));
+  CK(cudaMemsetAsync(g.F[1], 0, g.npitch * sizeof(float2), s));
+  CK(cudaMemsetAsync(g.coef, 0, g.npitch * kNumCoef * sizeof(float), s));
+
+  // Raw model arrays -> coefficients (temporary 6-volume buffer).
+  float *raw = nullptr;
+  CK(cudaMalloc(&raw, 6 * g.n * sizeof(float)));
+  const float *src6[6] = {vpz, vsv, epsilon, delta, phi, theta};
+  for (int k = 0; k < 6; ++k)
+    CK(cudaMemcpyAsync(raw + k * g.n, src6[k], g.n * sizeof(float), cudaMemcpyHostToDevice, s));
+  k_precompute<<<grid_for(g.n), 256, 0, s>>>(raw, g.coef, sx, sy, sz, g.pitch);
+  CK(cudaGetLastError());
+  // Initial fields (the reference's OpenMP back-end works on the caller's
+  // arrays, so their contents are the initial state).
+  g.cur = 0;
+  const float *fp[2][2] = {{pc, qc}, {pp, qp}};
+  for (int b = 0; b < 2; ++b) {
+    const float *p = fp[b][0], *q = fp[b][1];
+    if (p) CK(cudaMemcpyAsync(raw, p, g.n * sizeof(float), cudaMemcpyHostToDevice, s));
+    if (q) CK(cudaMemcpyAsync(raw + g.n, q, g.n * sizeof(float), cudaMemcpyHostToDevice, s));
+    k_pack<<<grid_for(g.n), 256, 0, s>>>(p ? raw : nullptr, q ? raw + g.n : nullptr, g.F[b], sx, sy, sz, g.pitch);
+    CK(cudaGetLastError());
+  }
+  CK(cudaStreamSynchronize(s));
+  CK(cudaFree(raw));
+
+  // Tensor maps.
+  const int TY = rows;
+  {
+    const cuuint64_t dims[3] = {(cuuint64_t)sx, (cuuint64_t)sy, (cuuint64_t)sz};
+    const cuuint64_t str[2] = {(cuuint64_t)g.pitch * 8, (cuuint64_t)g.pitch * sy * 8};
+    const cuuint32_t hbox[3] = {(cuuint32_t)(kTileX + 2 * kRadius), (cuuint32_t)(TY + 2 * kRadius), 1};
+    const cuuint32_t pbox[3] = {(cuuint32_t)kTileX, (cuuint32_t)TY, 1};
+    for (int b = 0; b < 2; ++b) {
+      if (encode(&g.halo[b], CU_TENSOR_MAP_DATA_TYPE_INT64, 3, g.F[b], dims, str, hbox)) return g_last_err;
+      if (encode(&g.pt[b], CU_TENSOR_MAP_DATA_TYPE_INT64, 3, g.F[b], dims, str, pbox)) return g_last_err;
+    }
+    const cuuint64_t cdims[4] = {(cuuint64_t)sx, (cuuint64_t)sy, (cuuint64_t)kNumCoef, (cuuint64_t)sz};
+    const cuuint64_t cstr[3] = {(cuuint64_t)g.pitch * 4, (cuuint64_t)g.pitch * sy * 4,
+                                (cuuint64_t)g.pitch * sy * kNumCoef * 4};
+    const cuuint32_t abox[4] = {(cuuint32_t)kTileX, (cuuint32_t)TY, (cuuint32_t)kArrivalCoef, 1};
+    const cuuint32_t ubox[4] = {(cuuint32_t)kTileX, (cuuint32_t)TY, (cuuint32_t)kUpdateCoef, 1};
+    if (encode(&g.arr, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, g.coef, cdims, cstr, abox)) return g_last_err;
+    if (encode(&g.upd, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, g.coef, cdims, cstr, ubox)) return g_last_err;
+  }
+  // Work decomposition.
+  g.ntx = (sx - bord - kRadius + kTileX - 1) / kTileX;
+  g.nty = (sy - bord - kRadius + TY - 1) / TY;
+  const int ctas = g.num_sms * propagate_fp32_ctas_per_sm(TY);
+  choose_chunks(ctas, g.ntx * g.nty, sz - 2 * bord, g.zchunks, &g.nchunk, &g.chunk);
+  g.nitems = g.ntx * g.nty * g.nchunk;
+  g.grid = g.nitems < ctas ? g.nitems : ctas;
+  g.launches = 0;
+  g.pending = Source();
+  g.owed = Source();
+  g.init = true;
+  return FLETCHER_OK;
+}
+
+// One step: source `pending` (if any) fused, then rotation.
+int step() {
+  PropLaunch L;
+  const int c = g.cur, p = 1 - g.cur;
+  L.cur_halo = g.halo[c];
+  L.prev_pt = g.pt[p];
+  L.coef_arr = g.arr;
+  L.coef_upd = g.upd;
+  L.tile_rows = g.tile_rows;
+  L.stages = g.stages;
+  L.grid = g.grid;
+  PropParams &P = L.p;
+  P.prev = g.F[p];
+  P.sx = g.sx; P.sy = g.sy; P.sz = g.sz; P.pitch = g.pitch; P.bord = g.bord;
+  P.ntx = g.ntx; P.nty = g.nty; P.nchunk = g.nchunk; P.chunk = g.chunk; P.nitems = g.nitems;
+  P.inv_dx = 1.0f / g.dx;
+  P.inv_dy = 1.0f / g.dy;
+  P.inv_dz = 1.0f / g.dz;
+  P.inv_dxx = 1.0f / (g.dx * g.dx);
+  P.inv_dyy = 1.0f / (g.dy * g.dy);
+  P.inv_dzz = 1.0f / (g.dz * g.dz);
+  P.dt2 = g.dt * g.dt;
+  P.src_x = P.src_y = P.src_z = -1000;
+  P.src = 0.f;
+  bool fused = false;
+  if (g.pending.on) {
+    if (in_update_region(g.pending.idx)) {
+      const long i = g.pending.idx;
+      P.src_x = (int)(i % g.sx);
+      P.src_y = (int)((i / g.sx) % g.sy);
+      P.src_z = (int)(i / ((long)g.sx * g.sy));
+      P.src = g.pending.val;
+      fused = true;
+    } else {
+      k_add_source<<<1, 32, 0, g_stream>>>(g.F[c], pitched_index(g.pending.idx), g.pending.val);
+      CK(cudaGetLastError());
+    }
+  }
+  P.cor_x = P.cor_y = P.cor_z = -1000;
+  P.cor = 0.f;
+  if (g.owed.on) {
+    const long i = g.owed.idx;
+    P.cor_x = (int)(i % g.sx);
+    P.cor_y = (int)((i / g.sx) % g.sy);
+    P.cor_z = (int)(i / ((long)g.sx * g.sy));
+    P.cor = g.owed.val;
+  }
+  P.err = g.err_dev;
+  CK(propagate_fp32_launch(L, g_stream));
+  ++g.launches;
+  // The buffer that was current becomes the previous field; it lacks the
+  // fused source, which the next step adds when it reads that cell.
+  g.owed = fused ? g.pending : Source();
+  g.pending = Source();
+  g.cur = p;
+  return FLETCHER_OK;
+}
+
+int read_component(const float2 *F, int comp, float *host) {
+  k_unpack<<<grid_for(g.n), 256, 0, g_stream>>>(F, g.scratch, comp, g.sx, g.sy, g.sz, g.pitch);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(host, g.scratch, g.n * sizeof(float), cudaMemcpyDeviceToHost, g_stream));
+  CK(cudaStreamSynchronize(g_stream));
+  return check_err_word();
+}
+
+}  // namespace
+
+// ===== Part 1 ====================================================================
+
+extern "C" void DRIVER_Initialize(const int sx, const int sy, const int sz, const int bord, float dx, float dy,
+                                  float dz, float dt, float *vpz, float *vsv, float *epsilon, float *delta,
+                                  float *phi, float *theta, float *pp, float *pc, float *qp, float *qc) {
+  if (initialize(sx, sy, sz, bord, dx, dy, dz, dt, vpz, vsv, epsilon, delta, phi, theta, pp, pc, qp, qc) !=
+      FLETCHER_OK)
+    free_state();
+}
+
+extern "C" void DRIVER_Finalize(void) {
+  if (g.init && g_stream) cudaStreamSynchronize(g_stream);
+  free_state();
+  if (g_own_stream && g_stream) {
+    cudaStreamDestroy(g_stream);
+    g_stream = nullptr;
+    g_own_stream = false;
+  }
+}
+
+extern "C" void DRIVER_Propagate(const int sx, const int sy, const int sz, const int bord, const float dx,
+                                 const float dy, const float dz, const float dt, const int it, float *pp, float *pc,
+                                 float *qp, float *qc) {
+  (void)bord; (void)dx; (void)dy; (void)dz; (void)dt; (void)it; (void)pp; (void)pc; (void)qp; (void)qc;
+  if (check_dims(sx, sy, sz)) return;
+  if (step()) return;
+  cudaError_t e = cudaStreamSynchronize(g_stream);
+  if (e != cudaSuccess) {
+    fail(FLETCHER_ERR_CUDA, "propagate step failed: %s", cudaGetErrorString(e));
+    return;
+  }
+  check_err_word();
+}
+
+extern "C" void DRIVER_Update_pointers(const int sx, const int sy, const int sz, float *pc) {
+  if (check_dims(sx, sy, sz) || !pc) return;
+  if (read_component(g.F[g.cur], 0, pc)) return;
+  if (g.pending.on) pc[g.pending.idx] = pc[g.pending.idx] + g.pending.val;
+}
+
+extern "C" void DRIVER_InsertSource(float dt, int it, int iSource, float *p, float *q, float src) {
+  (void)dt; (void)it; (void)p; (void)q;
+  if (!g.init) {
+    fail(FLETCHER_ERR_ARGS, "DRIVER_InsertSource before DRIVER_Initialize");
+    return;
+  }
+  if (iSource < 0 || (size_t)iSource >= g.n) {
+    fail(FLETCHER_ERR_ARGS, "source index %d outside the grid", iSource);
+    return;
+  }
+  if (g.pending.on) {
+    // A second source before the next step: store the first one now.
+    k_add_source<<<1, 32, 0, g_stream>>>(g.F[g.cur], pitched_index(g.pending.idx), g.pending.val);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      fail(FLETCHER_ERR_CUDA, "source kernel: %s", cudaGetErrorString(e));
+      return;
+    }
+  }
+  g.pending.on = true;
+  g.pending.idx = iSource;
+  g.pending.val = src;
+}
+
+// ===== Part 2 ====================================================================
+
+extern "C" void FLETCHER_SetErrorMode(int mode) { g_errmode = mode; }
+extern "C" int FLETCHER_GetLastError(void) { return g_last_err; }
+extern "C" const char *FLETCHER_GetLastErrorString(void) { return g_errmsg; }
+extern "C" void FLETCHER_ClearError(void) {
+  g_last_err = FLETCHER_OK;
+  g_errmsg[0] = 0;
+  if (g.err_host) *g.err_host = 0;
+}
+
+extern "C" int FLETCHER_SetStream(void *s) {
+  if (g_own_stream && g_stream) {
+    cudaStreamSynchronize(g_stream);
+    cudaStreamDestroy(g_stream);
+  }
+  g_stream = static_cast<cudaStream_t>(s);
+  g_own_stream = false;
+  return FLETCHER_OK;
+}
+extern "C" void *FLETCHER_GetStream(void) { return g_stream; }
+
+extern "C" int FLETCHER_SetForm(int form) {
+  if (form != FLETCHER_FORM_FP32) return fail(FLETCHER_ERR_ARGS, "unknown storage form %d", form);
+  g_form = form;
+  return FLETCHER_OK;
+}
+
+extern "C" int FLETCHER_SetTileConfig(int rows, int stages, int zchunks) {
+  const int r = rows ? rows : 12, s = stages ? stages : 4;
+  if (!propagate_fp32_supported(r, s)) return fail(FLETCHER_ERR_ARGS, "tile shape (%d, %d) is not built", r, s);
+  if (zchunks < 0) return fail(FLETCHER_ERR_ARGS, "zchunks must be >= 0");
+  g_req_rows = rows;
+  g_req_stages = stages;
+  g_req_chunks = zchunks;
+  return FLETCHER_OK;
+}
+
+extern "C" int FLETCHER_Run(int nsteps, long iSource, const float *src) {
+  if (!g.init) return fail(FLETCHER_ERR_ARGS, "FLETCHER_Run before DRIVER_Initialize");
+  if (iSource >= 0 && ((size_t)iSource >= g.n || !src)) return fail(FLETCHER_ERR_ARGS, "bad source");
+  for (int s = 0; s < nsteps; ++s) {
+    if (iSource >= 0) {
+      if (g.pending.on) {
+        k_add_source<<<1, 32, 0, g_stream>>>(g.F[g.cur], pitched_index(g.pending.idx), g.pending.val);
+        CK(cudaGetLastError());
+      }
+      g.pending.on = true;
+      g.pending.idx = iSource;
+      g.pending.val = src[s];
+    }
+    if (step()) return g_last_err;
+  }
+  return FLETCHER_OK;
+}
+
+extern "C" int FLETCHER_Synchronize(void) {
+  if (!g_stream) return FLETCHER_OK;
+  CK(cudaStreamSynchronize(g_stream));
+  return check_err_word();
+}
+
+extern "C" int FLETCHER_GetField(int which, float *host) {
+  if (!g.init) return fail(FLETCHER_ERR_ARGS, "FLETCHER_GetField before DRIVER_Initialize");
+  if (which < 0 || which > 3 || !host) return fail(FLETCHER_ERR_ARGS, "bad field selector %d", which);
+  const int buf = which < 2 ? g.cur : 1 - g.cur;
+  if (read_component(g.F[buf], which & 1, host)) return g_last_err;
+  const Source &fix = which < 2 ? g.pending : g.owed;
+  if (fix.on) host[fix.idx] = host[fix.idx] + fix.val;
+  return FLETCHER_OK;
+}
+
+extern "C" int FLETCHER_GetCoefficients(float *host) {
+  if (!g.init) return fail(FLETCHER_ERR_ARGS, "FLETCHER_GetCoefficients before DRIVER_Initialize");
+  // Reference declaration order: ch1dxx ch1dyy ch1dzz ch1dxy ch1dyz ch1dxz v2px v2pz v2sz v2pn.
+  const int order[kNumCoef] = {DC_XX, DC_YY, DC_ZZ, DC_XY, DC_YZ, DC_XZ, DC_V2PX, DC_V2PZ, DC_V2SZ, DC_V2PN};
+  for (int k = 0; k < kNumCoef; ++k) {
+    k_unpack_coef<<<grid_for(g.n), 256, 0, g_stream>>>(g.coef, g.scratch, order[k], g.sx, g.sy, g.sz, g.pitch);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(host + k * g.n, g.scratch, g.n * sizeof(float), cudaMemcpyDeviceToHost, g_stream));
+  }
+  CK(cudaStreamSynchronize(g_stream));
+  return FLETCHER_OK;
+}
+
+extern "C" long FLETCHER_KernelLaunches(void) { return g.launches; }
+extern "C" size_t FLETCHER_DeviceBytes(void) { return g.dev_bytes; }
+extern "C" double FLETCHER_BytesPerCell(void) {
+  // current (p,q) 8 B + previous (p,q) 8 B + ten coefficients 40 B + next (p,q) 8 B.
+  return 64.0;
+}

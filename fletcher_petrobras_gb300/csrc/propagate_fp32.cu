@@ -1,0 +1,363 @@
+// Plain FP32 Fletcher TTI step for sm_103a.
+//
+// Computes, for every cell of [bord, s-bord)^3, the coupled p/q update of
+// original/sample.h:32-89 (Der2 / DerCross of original/derivatives.h:37-68,
+// weighted by the ch1d** and v2** coefficients of original/precomp.h), with
+// the source of original/OpenMP/openmp_insertsource.c:7-13 fused in.
+//
+// Structure (one CTA per SM, persistent):
+//  * a work item is a 32 x TY column tile of one z-chunk; the CTA streams
+//    its planes k = z0-4 .. z1+3 in z;
+//  * thread 0 issues TMA loads S-1 planes ahead into a ring of shared-memory
+//    stages: the (p,q) halo tile of plane k (box 40 x (TY+8)), the three
+//    in-plane coefficients of plane k, and the seven other coefficients and
+//    the previous (p,q) of plane k-4, which is updated at this step;
+//  * each thread owns one (x, y) column.  When plane k arrives it reads its
+//    9-point x and y neighbourhoods from shared memory and forms Der2x,
+//    Der2y and the first derivatives D1x, D1y; DerCross xy is D1x applied to
+//    D1y (exchanged through shared memory, including the 4-column x halo);
+//    DerCross xz and yz are the z first derivative of the D1x / D1y values,
+//    which each thread keeps for 9 planes in registers, as it keeps p and q
+//    for Der2z;
+//  * both fields travel as one 64-bit (p, q) pair and are updated with the
+//    packed .f32x2 add/mul/fma instructions;
+//  * plane k-4 is completed at step k and written with coalesced 64-bit
+//    stores into the previous-field buffer (in place).
+//
+// DerCross(p, a, b) equals D1_b(D1_a(p)) exactly in real arithmetic because
+// its weights are the products L_i L_j of the first-derivative weights
+// (original/derivatives.h:13-31); the FP32 rounding differs from the
+// reference's grouped sum, which the parity tolerance covers.
+#include "device_util.cuh"
+#include "fletcher_internal.h"
+
+namespace flt {
+
+template <int TY>
+struct Geo {
+  static constexpr int TX = kTileX;
+  static constexpr int HX = TX + 2 * kRadius;
+  static constexpr int HY = TY + 2 * kRadius;
+  static constexpr int NT = TX * TY;
+  static constexpr int HALO_B = HX * HY * 8;
+  static constexpr int ARR_B = kArrivalCoef * NT * 4;
+  static constexpr int UPD_B = kUpdateCoef * NT * 4;
+  static constexpr int PP_B = NT * 8;
+  static constexpr int OFF_ARR = HALO_B;
+  static constexpr int OFF_UPD = OFF_ARR + ARR_B;
+  static constexpr int OFF_PP = OFF_UPD + UPD_B;
+  static constexpr int STAGE_B = (OFF_PP + PP_B + 127) / 128 * 128;
+  static constexpr int DBUF_B = 2 * TY * HX * 8;
+  static_assert(TY % 4 == 0, "tile rows must be a multiple of 4");
+  static_assert(HALO_B % 128 == 0 && ARR_B % 128 == 0 && UPD_B % 128 == 0, "stage regions 128-B aligned");
+};
+
+template <int TY, int S>
+constexpr size_t smem_bytes() {
+  return size_t(S) * Geo<TY>::STAGE_B + Geo<TY>::DBUF_B + 8 * S + 128;
+}
+
+struct Item {
+  int x0, y0, z0, z1;
+};
+
+template <int TY>
+__device__ __forceinline__ Item decode_item(int item, const PropParams &P) {
+  Item it;
+  const int tx = item % P.ntx;
+  const int r = item / P.ntx;
+  const int ty = r % P.nty;
+  const int ch = r / P.nty;
+  it.x0 = kRadius + tx * kTileX;
+  it.y0 = kRadius + ty * TY;
+  it.z0 = P.bord + ch * P.chunk;
+  it.z1 = min(it.z0 + P.chunk, P.sz - P.bord);
+  return it;
+}
+
+__device__ __forceinline__ f2 ldw(const float2 &w) { return *reinterpret_cast<const f2 *>(&w); }
+
+// Thread 0's side of the pipeline: issues the TMA loads of one step.
+template <int TY>
+__device__ __forceinline__ void issue_step(unsigned char *stage, uint64_t *bar, const Item &it, int k,
+                                           const CUtensorMap *tm_cur, const CUtensorMap *tm_prev,
+                                           const CUtensorMap *tm_arr, const CUtensorMap *tm_upd) {
+  using G = Geo<TY>;
+  const bool center = (k >= it.z0) && (k < it.z1);
+  const bool upd = (k - kRadius >= it.z0);
+  const uint32_t bytes = G::HALO_B + (center ? G::ARR_B : 0) + (upd ? G::UPD_B + G::PP_B : 0);
+  mbar_arrive_expect_tx(bar, bytes);
+  tma_load_3d(stage, tm_cur, bar, it.x0 - kRadius, it.y0 - kRadius, k);
+  if (center) tma_load_4d(stage + G::OFF_ARR, tm_arr, bar, it.x0, it.y0, 0, k);
+  if (upd) {
+    tma_load_4d(stage + G::OFF_UPD, tm_upd, bar, it.x0, it.y0, kArrivalCoef, k - kRadius);
+    tma_load_3d(stage + G::OFF_PP, tm_prev, bar, it.x0, it.y0, k - kRadius);
+  }
+}
+
+// Stencil weights of original/derivatives.h:13-41 (first derivative L1..L4,
+// second derivative K0..K4), as compile-time constants; the 1/d and 1/d^2
+// factors are applied once per derivative.
+constexpr float cL1 = 0.8f, cL2 = -0.2f, cL3 = 0.0380952380952381f, cL4 = -0.0035714285714285713f;
+constexpr float cK0 = -2.84722222222222222222f, cK1 = 1.6f, cK2 = -0.2f, cK3 = 0.02539682539682539682f,
+                cK4 = -0.00178571428571428571f;
+
+// First derivative (unscaled) from the four (+j, -j) pairs.
+__device__ __forceinline__ f2 d1(f2 a1, f2 b1, f2 a2, f2 b2, f2 a3, f2 b3, f2 a4, f2 b4) {
+  f2 r = mul2(splat(cL1), sub2(a1, b1));
+  r = fma2(splat(cL2), sub2(a2, b2), r);
+  r = fma2(splat(cL3), sub2(a3, b3), r);
+  return fma2(splat(cL4), sub2(a4, b4), r);
+}
+// Second derivative (unscaled) from the centre and four (+j, -j) pairs.
+__device__ __forceinline__ f2 d2(f2 c, f2 a1, f2 b1, f2 a2, f2 b2, f2 a3, f2 b3, f2 a4, f2 b4) {
+  f2 r = mul2(splat(cK0), c);
+  r = fma2(splat(cK1), add2(a1, b1), r);
+  r = fma2(splat(cK2), add2(a2, b2), r);
+  r = fma2(splat(cK3), add2(a3, b3), r);
+  return fma2(splat(cK4), add2(a4, b4), r);
+}
+
+// Next step the producer must load: `ahead` steps after step k of `item`.
+// Returns false when the CTA has no such step.
+template <int TY>
+__device__ __forceinline__ bool step_after(const PropParams &P, int item, int k, int ahead, Item &out_it,
+                                           int &out_k) {
+  Item it = decode_item<TY>(item, P);
+  int kk = k + ahead;
+  while (kk >= it.z1 + kRadius) {
+    const int over = kk - (it.z1 + kRadius);
+    item += gridDim.x;
+    if (item >= P.nitems) return false;
+    it = decode_item<TY>(item, P);
+    kk = it.z0 - kRadius + over;
+  }
+  out_it = it;
+  out_k = kk;
+  return true;
+}
+
+template <int TY, int S, int MINB>
+__global__ void __launch_bounds__(kTileX *TY, MINB)
+    k_propagate_fp32(const __grid_constant__ CUtensorMap tm_cur, const __grid_constant__ CUtensorMap tm_prev,
+                     const __grid_constant__ CUtensorMap tm_arr, const __grid_constant__ CUtensorMap tm_upd,
+                     const PropParams P) {
+  using G = Geo<TY>;
+  extern __shared__ unsigned char smem_dyn[];
+  unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_dyn) + 127) & ~uintptr_t(127));
+  f2 *dbuf = reinterpret_cast<f2 *>(smem + S * G::STAGE_B);
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + S * G::STAGE_B + G::DBUF_B);
+  __shared__ int s_abort;
+
+  const int tid = threadIdx.x;
+  const int lx = tid & 31;
+  const int ly = tid >> 5;
+
+  if (blockIdx.x >= P.nitems) return;
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
+    mbar_fence_init();
+    s_abort = 0;
+    tma_prefetch_desc(&tm_cur);
+    tma_prefetch_desc(&tm_prev);
+    tma_prefetch_desc(&tm_arr);
+    tma_prefetch_desc(&tm_upd);
+    // Prologue: the first S-1 steps of this CTA.
+    const Item i0 = decode_item<TY>(blockIdx.x, P);
+    for (int a = 0; a < S - 1; ++a) {
+      Item it;
+      int k;
+      if (!step_after<TY>(P, blockIdx.x, i0.z0 - kRadius, a, it, k)) break;
+      issue_step<TY>(smem + a * G::STAGE_B, &full[a], it, k, &tm_cur, &tm_prev, &tm_arr, &tm_upd);
+    }
+  }
+  __syncthreads();
+
+  int stage = 0;
+  uint32_t phase = 0;
+  int dsel = 0;
+  for (int item = blockIdx.x; item < P.nitems; item += gridDim.x) {
+    const Item it = decode_item<TY>(item, P);
+    const int kbeg = it.z0 - kRadius;
+    const int kend = it.z1 + kRadius;
+    const int gx = it.x0 + lx;
+    const int gy = it.y0 + ly;
+    const bool valid = (gx >= P.bord) && (gx < P.sx - P.bord) && (gy >= P.bord) && (gy < P.sy - P.bord);
+    const int ci = ly * G::TX + lx;
+    const int hc = (ly + kRadius) * G::HX + (lx + kRadius);
+
+    f2 Pr[9], Dx[9], Dy[9], A[9], B[9];
+
+    for (int kb = kbeg; kb < kend; kb += 9) {
+#pragma unroll
+      for (int j = 0; j < 9; ++j) {
+        const int k = kb + j;
+        if (k >= kend) break;
+        unsigned char *st = smem + stage * G::STAGE_B;
+        if (!mbar_wait(&full[stage], phase, kWaitLimitNs)) {
+          s_abort = 1;
+          atomicOr(P.err, 1u);
+        }
+        const bool center = (k >= it.z0) && (k < it.z1);
+        const bool upd = (k - kRadius >= it.z0);
+
+        // Fused source: add to the (p, q) of the source cell in this CTA's
+        // copy of the plane before any thread reads it.
+        if (k == P.src_z) {
+          const int hx = P.src_x - (it.x0 - kRadius);
+          const int hy = P.src_y - (it.y0 - kRadius);
+          if (hx >= 0 && hx < G::HX && hy >= 0 && hy < G::HY) {
+            __syncthreads();
+            if (tid == 0) {
+              f2 *h = reinterpret_cast<f2 *>(st) + hy * G::HX + hx;
+              *h = add2(*h, splat(P.src));
+            }
+            __syncthreads();
+          }
+        }
+
+        const f2 *H = reinterpret_cast<const f2 *>(st);
+        const f2 c = H[hc];
+        f2 d1x, d1y, d2x, d2y;
+        {
+          const f2 a1 = H[hc + 1], b1 = H[hc - 1], a2 = H[hc + 2], b2 = H[hc - 2];
+          const f2 a3 = H[hc + 3], b3 = H[hc - 3], a4 = H[hc + 4], b4 = H[hc - 4];
+          d1x = mul2(splat(P.inv_dx), d1(a1, b1, a2, b2, a3, b3, a4, b4));
+          if (center) d2x = mul2(splat(P.inv_dxx), d2(c, a1, b1, a2, b2, a3, b3, a4, b4));
+        }
+        {
+          constexpr int W = G::HX;
+          const f2 a1 = H[hc + W], b1 = H[hc - W], a2 = H[hc + 2 * W], b2 = H[hc - 2 * W];
+          const f2 a3 = H[hc + 3 * W], b3 = H[hc - 3 * W], a4 = H[hc + 4 * W], b4 = H[hc - 4 * W];
+          d1y = mul2(splat(P.inv_dy), d1(a1, b1, a2, b2, a3, b3, a4, b4));
+          if (center) d2y = mul2(splat(P.inv_dyy), d2(c, a1, b1, a2, b2, a3, b3, a4, b4));
+        }
+        Pr[j] = c;
+        Dx[j] = d1x;
+        Dy[j] = d1y;
+
+        f2 *db = dbuf + dsel * (TY * G::HX);
+        if (center) {
+          db[ly * G::HX + lx + kRadius] = d1y;
+          if (ly < TY / 4) {
+            // D1y in the 4-column x halo on each side, for DerCross xy.
+            const int r = ly * 4 + (lx >> 3);
+            const int cc = lx & 7;
+            const int hxc = cc < 4 ? cc : G::TX + cc;
+            const int hh = (r + kRadius) * G::HX + hxc;
+            constexpr int W = G::HX;
+            db[r * G::HX + hxc] =
+                mul2(splat(P.inv_dy), d1(H[hh + W], H[hh - W], H[hh + 2 * W], H[hh - 2 * W], H[hh + 3 * W],
+                                         H[hh - 3 * W], H[hh + 4 * W], H[hh - 4 * W]));
+          }
+        }
+        __syncthreads();
+        if (s_abort) {
+          if (tid == 0) {
+            // Drain the loads still in flight (bounded) before leaving.
+            int s2 = stage;
+            uint32_t ph2 = phase;
+            for (int a = 0; a < S - 1; ++a) {
+              Item it2;
+              int k2;
+              if (!step_after<TY>(P, item, k, a, it2, k2)) break;
+              (void)mbar_wait(&full[s2], ph2, kWaitLimitNs);
+              if (++s2 == S) { s2 = 0; ph2 ^= 1u; }
+            }
+          }
+          return;
+        }
+        if (tid == 0) {
+          // Refill the stage consumed at the previous step (all threads are
+          // past it) with the step S-1 ahead.
+          Item it2;
+          int k2;
+          if (step_after<TY>(P, item, k, S - 1, it2, k2)) {
+            const int s2 = (stage + S - 1) % S;
+            fence_proxy_async_smem();
+            issue_step<TY>(smem + s2 * G::STAGE_B, &full[s2], it2, k2, &tm_cur, &tm_prev, &tm_arr, &tm_upd);
+          }
+        }
+        if (center) {
+          const f2 *dr = db + ly * G::HX + lx + kRadius;
+          const f2 dxy = mul2(splat(P.inv_dx), d1(dr[1], dr[-1], dr[2], dr[-2], dr[3], dr[-3], dr[4], dr[-4]));
+          const float *ca = reinterpret_cast<const float *>(st + G::OFF_ARR);
+          const float cxx = ca[ci], cyy = ca[G::NT + ci], cxy = ca[2 * G::NT + ci];
+          A[j] = fma2(splat(cxy), dxy, fma2(splat(cyy), d2y, mul2(splat(cxx), d2x)));
+          B[j] = add2(d2x, d2y);
+        }
+        if (upd) {
+          const int cs = (j + 5) % 9;  // ring slot of plane k-4
+#define RP(o) Pr[(cs + (o)) % 9]
+#define RX(o) Dx[(cs + (o)) % 9]
+#define RY(o) Dy[(cs + (o)) % 9]
+          const f2 d2z = mul2(splat(P.inv_dzz), d2(RP(0), RP(1), RP(8), RP(2), RP(7), RP(3), RP(6), RP(4), RP(5)));
+          const f2 dxz = mul2(splat(P.inv_dz), d1(RX(1), RX(8), RX(2), RX(7), RX(3), RX(6), RX(4), RX(5)));
+          const f2 dyz = mul2(splat(P.inv_dz), d1(RY(1), RY(8), RY(2), RY(7), RY(3), RY(6), RY(4), RY(5)));
+#undef RP
+#undef RX
+#undef RY
+          const float *cu = reinterpret_cast<const float *>(st + G::OFF_UPD);
+          const float czz = cu[ci], cxz = cu[G::NT + ci], cyz = cu[2 * G::NT + ci];
+          const float v2px = cu[3 * G::NT + ci], v2pz = cu[4 * G::NT + ci];
+          const float v2sz = cu[5 * G::NT + ci], v2pn = cu[6 * G::NT + ci];
+          const f2 h1 = fma2(splat(cyz), dyz, fma2(splat(cxz), dxz, fma2(splat(czz), d2z, A[cs])));
+          const f2 h2 = sub2(add2(B[cs], d2z), h1);
+          const float h1p = lo(h1), h1q = hi(h1), h2p = lo(h2), h2q = hi(h2);
+          const float rhsp = v2px * h2p + v2pz * h1q + v2sz * (h1p - h1q);
+          const float rhsq = v2pn * h2p + v2pz * h1q - v2sz * (h2p - h2q);
+          f2 old = reinterpret_cast<const f2 *>(st + G::OFF_PP)[ci];
+          const int zc = k - kRadius;
+          if (zc == P.cor_z && gx == P.cor_x && gy == P.cor_y) old = add2(old, splat(P.cor));
+          const f2 cur = Pr[cs];
+          const f2 nw = fma2(mk2(rhsp, rhsq), splat(P.dt2), sub2(add2(cur, cur), old));
+          if (valid) {
+            reinterpret_cast<unsigned long long *>(P.prev)[((long)zc * P.sy + gy) * P.pitch + gx] = nw.v;
+          }
+        }
+        dsel ^= 1;
+        if (++stage == S) {
+          stage = 0;
+          phase ^= 1u;
+        }
+      }
+    }
+  }
+}
+
+// ---- host side ---------------------------------------------------------------
+
+template <int TY, int S, int MINB>
+static cudaError_t launch_t(const PropLaunch &L, cudaStream_t s) {
+  constexpr size_t smem = smem_bytes<TY, S>();
+  auto kern = k_propagate_fp32<TY, S, MINB>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  kern<<<L.grid, kTileX * TY, smem, s>>>(L.cur_halo, L.prev_pt, L.coef_arr, L.coef_upd, L.p);
+  return cudaGetLastError();
+}
+
+// Supported shapes: rows per tile x stages.  TY = 16 runs one 512-thread CTA
+// per SM; TY = 8 runs two 256-thread CTAs per SM.
+#define FLT_SHAPES(X) X(16, 4, 1) X(16, 5, 1) X(16, 3, 1) X(8, 4, 2) X(8, 3, 2) X(12, 4, 1)
+
+size_t propagate_fp32_smem_bytes(int ty, int st) {
+#define X(a, b, c) \
+  if (ty == a && st == b) return smem_bytes<a, b>();
+  FLT_SHAPES(X)
+#undef X
+  return 0;
+}
+bool propagate_fp32_supported(int ty, int st) { return propagate_fp32_smem_bytes(ty, st) != 0; }
+int propagate_fp32_threads(int ty) { return kTileX * ty; }
+int propagate_fp32_ctas_per_sm(int ty) { return ty == 8 ? 2 : 1; }
+
+cudaError_t propagate_fp32_launch(const PropLaunch &L, cudaStream_t s) {
+#define X(a, b, c) \
+  if (L.tile_rows == a && L.stages == b) return launch_t<a, b, c>(L, s);
+  FLT_SHAPES(X)
+#undef X
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace flt

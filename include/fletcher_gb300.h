@@ -1,0 +1,175 @@
+/*
+ * fletcher_gb300.h -- C ABI of libfletcher_gb300.so, the GB300 (sm_103a)
+ * back-end of the Fletcher TTI pseudo-acoustic propagator.
+ *
+ * Part 1 is the reference's five-function back-end interface, with the
+ * same names, argument meaning and ownership rules, so the reference's
+ * front-end (main.c, model.c, boundary.c, source.c, utils.c, map.c,
+ * walltime.c) links against this library in place of its OpenMP or CUDA
+ * back-end objects.  Part 2 holds extension entry points (error status,
+ * launch stream, multi-step runs, field read-back); part 3 the host-side
+ * model preparation and time loop this library ships for its own
+ * front-end.  All pointers are plain host pointers unless stated.
+ */
+#ifndef FLETCHER_GB300_H
+#define FLETCHER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ===== Part 1: the reference back-end interface ========================= */
+
+/* Replaces original/driver.h:8-12.  Copies the six raw model arrays and the
+ * four initial fields (sx*sy*sz floats each, x fastest) to the GPU, computes
+ * the ten coefficient fields there in FP64 (original/precomp.h:14-58) and
+ * keeps everything resident.  Requires bord >= 4 (the stencil radius). */
+void DRIVER_Initialize(const int sx, const int sy, const int sz, const int bord, float dx,
+                       float dy, float dz, float dt, float *vpz, float *vsv, float *epsilon,
+                       float *delta, float *phi, float *theta, float *pp, float *pc, float *qp,
+                       float *qc);
+
+/* Replaces original/driver.h:14.  Frees all device state. */
+void DRIVER_Finalize(void);
+
+/* Replaces original/driver.h:16-18.  Advances p and q one time step over
+ * the cells [bord, s-bord) of each axis and rotates the device buffers, as
+ * original/OpenMP/openmp_propagate.c:9-41 with original/sample.h:32-89 does.
+ * A source registered by DRIVER_InsertSource since the last step is applied
+ * inside the same kernel.  The host field pointers are not read (the
+ * device holds the state, as in original/CUDA/cuda_driver.c:78-88); the call
+ * returns after the step has completed. */
+void DRIVER_Propagate(const int sx, const int sy, const int sz, const int bord, const float dx,
+                      const float dy, const float dz, const float dt, const int it, float *pp,
+                      float *pc, float *qp, float *qc);
+
+/* Replaces original/driver.h:20.  Writes the current p field into host pc
+ * (sx*sy*sz floats), as original/CUDA/cuda_stuff.cu:195-201 does. */
+void DRIVER_Update_pointers(const int sx, const int sy, const int sz, float *pc);
+
+/* Replaces original/driver.h:22.  Adds src to the current p and q at linear
+ * index iSource (original/OpenMP/openmp_insertsource.c:7-13); the addition
+ * is fused into the next DRIVER_Propagate. */
+void DRIVER_InsertSource(float dt, int it, int iSource, float *p, float *q, float src);
+
+/* ===== Part 2: extension entry points (this library only) ================ */
+
+/* Error handling.  The reference's back-ends print and exit(1) on a CUDA
+ * error (original/CUDA/cuda_defines.h:14-20); that is the default here
+ * (FLETCHER_ERRMODE_EXIT).  FLETCHER_ERRMODE_RETURN prints, records a sticky
+ * status and returns instead. */
+#define FLETCHER_ERRMODE_EXIT 0
+#define FLETCHER_ERRMODE_RETURN 1
+#define FLETCHER_OK 0
+#define FLETCHER_ERR_ARGS 1      /* invalid sizes, indices or call order */
+#define FLETCHER_ERR_CUDA 2      /* a CUDA runtime call failed */
+#define FLETCHER_ERR_TIMEOUT 3   /* a kernel's bounded wait gave up */
+#define FLETCHER_ERR_NOMEM 4     /* device allocation failed */
+void FLETCHER_SetErrorMode(int mode);
+int FLETCHER_GetLastError(void);
+const char *FLETCHER_GetLastErrorString(void);
+void FLETCHER_ClearError(void);
+
+/* Stream on which every kernel and copy is issued (a cudaStream_t; NULL =
+ * the library's own stream).  Set before DRIVER_Initialize or between
+ * steps. */
+int FLETCHER_SetStream(void *cuda_stream);
+void *FLETCHER_GetStream(void);
+
+/* Storage form of the wave fields, chosen before DRIVER_Initialize.
+ * FLETCHER_FORM_FP32: p,q in FP32 (the reference's precision). */
+#define FLETCHER_FORM_FP32 0
+int FLETCHER_SetForm(int form);
+
+/* Kernel shape override for tuning (0 keeps the default): rows per tile,
+ * pipeline stages, z-chunks per column. */
+int FLETCHER_SetTileConfig(int tile_rows, int stages, int zchunks);
+
+/* Runs nsteps steps back to back on the stream without host
+ * synchronisation: step s adds src[s] at iSource (iSource < 0: no source),
+ * then propagates.  Equivalent to nsteps x (DRIVER_InsertSource +
+ * DRIVER_Propagate + swap).  Returns a FLETCHER_* status. */
+int FLETCHER_Run(int nsteps, long iSource, const float *src);
+
+/* Waits for the stream; returns a FLETCHER_* status (including a kernel's
+ * timeout flag). */
+int FLETCHER_Synchronize(void);
+
+/* Copies one field to host memory (sx*sy*sz floats): which = 0 current p,
+ * 1 current q, 2 previous p, 3 previous q. */
+int FLETCHER_GetField(int which, float *host);
+
+/* Copies the ten coefficient fields to host memory (10*sx*sy*sz floats) in
+ * the order ch1dxx ch1dyy ch1dzz ch1dxy ch1dyz ch1dxz v2px v2pz v2sz v2pn
+ * (original/precomp.h:14-58). */
+int FLETCHER_GetCoefficients(float *host);
+
+/* Number of propagate-kernel launches issued since DRIVER_Initialize. */
+long FLETCHER_KernelLaunches(void);
+
+/* Device bytes held by the current state. */
+size_t FLETCHER_DeviceBytes(void);
+
+/* Algorithmic HBM bytes one updated cell costs in the current form (reads
+ * of the current and previous fields and the coefficients, writes of the
+ * next field). */
+double FLETCHER_BytesPerCell(void);
+
+/* ===== Part 3: host-side model preparation and time loop ================= */
+
+/* Fills the six model arrays (vpz vsv epsilon delta phi theta, n floats
+ * each, consecutive in `model`) with one homogeneous medium; angles in
+ * radians. */
+void FLETCHER_ModelHomogeneous(long n, float vpz, float vsv, float epsilon, float delta,
+                               float phi, float theta, float *model);
+
+/* Horizontally layered TTI medium over the whole grid: `nlayers` layers of
+ * seeded random thickness that tile the interior depth nz, vpz drawn in
+ * [vmin, vmax] and sorted to increase with depth, epsilon ~ U[0, 0.3],
+ * delta ~ U[0, epsilon], theta ~ U[0, 45 deg], phi ~ U[0, 90 deg],
+ * vsv = vs_ratio * vpz.  Cells above / below the interior take the first /
+ * last layer.  The six arrays are consecutive in `model`.  Draws come from
+ * a splitmix64 stream seeded by `seed`, so results are identical on every
+ * platform.  layer_top (nlayers ints, may be NULL) receives each layer's
+ * first interior z index. */
+void FLETCHER_ModelLayered(int sx, int sy, int sz, int bord, int absorb, int nlayers,
+                           uint64_t seed, float vmin, float vmax, float vs_ratio, float *model,
+                           int *layer_top);
+
+/* RandomVelocityBoundary, as original/boundary.c:7-98: random-velocity
+ * absorbing zone of width `absorb` and a zero-velocity `bord` shell, drawn
+ * with the C library rand() after srand(seed). */
+void FLETCHER_RandomVelocityBoundary(int sx, int sy, int sz, int nx, int ny, int nz, int bord,
+                                     int absorb, float *vpz, float *vsv, unsigned seed);
+
+/* Ricker source value at time it*dt (original/source.c:7-15) for cut
+ * frequency fcut (original/source.h:11 fixes 40); peak frequency fcut/3. */
+float FLETCHER_Source(float dt, int it, double fcut);
+
+/* Advisory time step (original/main.c:225-239). */
+float FLETCHER_RecommendedDt(long n, const float *vpz, const float *epsilon, float dx, float dy,
+                             float dz);
+
+/* The time loop of original/model.c:32-164 through Part 1: coefficient set-up
+ * and DRIVER_Initialize, then for it = 1..st DRIVER_InsertSource with the
+ * source for time (it-1)*dt, DRIVER_Propagate and the pointer swap (the
+ * timed region, as original/model.c:82-88), and DRIVER_Update_pointers of
+ * the current p every dt_output seconds of simulated time (dt_output <= 0:
+ * never).  The final current p and q are copied to pc and qc, and
+ * DRIVER_Finalize is called.  Results in stats (may be NULL):
+ * stats[0] = propagate wall seconds, stats[1] = MSamples/s by the
+ * reference's definition, stats[2] = whole-call wall seconds, stats[3] =
+ * host-to-device bytes, stats[4] = device-to-host bytes.  Returns a
+ * FLETCHER_* status. */
+int FLETCHER_Model(int st, long iSource, double fcut, float dt_output, int sx, int sy, int sz,
+                   int bord, float dx, float dy, float dz, float dt, float *pp, float *pc,
+                   float *qp, float *qc, float *vpz, float *vsv, float *epsilon, float *delta,
+                   float *phi, float *theta, double *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
