@@ -160,6 +160,17 @@ class ClockSampler:
                 "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
 
 
+def workload(args):
+    """The C1 problem, or the same generator at another interior size (profiling)."""
+    from fletcher_petrobras_gb300 import C1
+
+    if args.interior == C1.nx:
+        return C1
+    n = args.interior
+    s = n + 2 * (C1.bord + C1.absorb)
+    return C1.with_(name=f"C1-layered-{n}", nx=n, ny=n, nz=n, source=(s // 2, s // 2, C1.bord + C1.absorb + 8))
+
+
 def run_gb300(args, ws, rank, local, group):
     import torch
 
@@ -168,7 +179,7 @@ def run_gb300(args, ws, rank, local, group):
 
     torch.cuda.set_device(local)
     lib = load()
-    prob = C1
+    prob = workload(args)
     K, W = args.steps, args.warmup
     model = prob.model()
     src = prob.sources(W + K)
@@ -207,18 +218,19 @@ def run_gb300(args, ws, rank, local, group):
     # End to end through the C ABI with host buffers (the reference's Model() sequence).
     import ctypes as C
 
-    n = prob.n
-    f = np.zeros((4, n), np.float32)
     stats = (C.c_double * 5)()
-    group.barrier()
-    rc = lib.FLETCHER_Model(K, prob.i_source, prob.fcut, 0.01, prob.sx, prob.sy, prob.sz, prob.bord, prob.dx,
-                            prob.dy, prob.dz, prob.dt, *[fptr(f[k]) for k in range(4)],
-                            *[fptr(model[k]) for k in range(6)], stats)
-    if rc:
-        raise RuntimeError("FLETCHER_Model failed: " + lib.FLETCHER_GetLastErrorString().decode())
-    e2e_wall = group.reduce(stats[2], "max")
-    e2e = ws * cells * K / e2e_wall / 1e6
-    del f
+    e2e = e2e_wall = None
+    if not args.no_e2e:
+        f = np.zeros((4, prob.n), np.float32)
+        group.barrier()
+        rc = lib.FLETCHER_Model(K, prob.i_source, prob.fcut, 0.01, prob.sx, prob.sy, prob.sz, prob.bord, prob.dx,
+                                prob.dy, prob.dz, prob.dt, *[fptr(f[k]) for k in range(4)],
+                                *[fptr(model[k]) for k in range(6)], stats)
+        if rc:
+            raise RuntimeError("FLETCHER_Model failed: " + lib.FLETCHER_GetLastErrorString().decode())
+        e2e_wall = group.reduce(stats[2], "max")
+        e2e = ws * cells * K / e2e_wall / 1e6
+        del f
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -236,8 +248,8 @@ def run_gb300(args, ws, rank, local, group):
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
         "ms_per_step": round(ms_max / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded 8-layer TTI model, random-velocity boundary)",
-        "config": {"workload": "C1: plain FP32 single shot, 504^3 interior (576^3 grid), bord 4, absorb 32, "
-                               "dx 12.5 m, dt 0.6 ms, 8-layer seeded TTI, 15 Hz Ricker at (288,288,44)",
+        "config": {"workload": f"C1: plain FP32 single shot, {prob.nx}^3 interior ({prob.sx}^3 grid), bord 4, "
+                               f"absorb 32, dx 12.5 m, dt 0.6 ms, 8-layer seeded TTI, 15 Hz Ricker at {prob.src_xyz}",
                    "grid": [prob.sx, prob.sy, prob.sz], "updated_cells_per_step": cells,
                    "form": "fp32", "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": f"inputs resident in HBM ({dev_gb:.1f} GB) are larger than L2 (129 MB); no flush",
@@ -248,7 +260,8 @@ def run_gb300(args, ws, rank, local, group):
                      "traffic": None if tpc is None else round(tpc * cells / 1e9, 3),
                      "traffic_unit": "GB per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
                      "kernel": "k_propagate_fp32"},
-        "e2e": {"value": round(e2e, 1), "unit": UNIT, "h2d_bytes_per_step": int(stats[3] / K),
+        "e2e": None if e2e is None else {
+                "value": round(e2e, 1), "unit": UNIT, "h2d_bytes_per_step": int(stats[3] / K),
                 "d2h_bytes_per_step": int(stats[4] / K), "wall_s": round(e2e_wall, 3),
                 "what": "FLETCHER_Model via the C ABI: DRIVER_Initialize (H2D of 6 model + 4 field arrays, "
                         "FP64 coefficient precompute) + K x (InsertSource, Propagate) + D2H snapshot of p every "
@@ -299,6 +312,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--interior", type=int, default=504, help="interior size n (n^3); 504 is the workload")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

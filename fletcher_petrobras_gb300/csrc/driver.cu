@@ -378,7 +378,10 @@ int step() {
   P.inv_dxx = 1.0f / (g.dx * g.dx);
   P.inv_dyy = 1.0f / (g.dy * g.dy);
   P.inv_dzz = 1.0f / (g.dz * g.dz);
-  P.dt2 = g.dt * g.dt;
+  // On an isotropic grid every derivative carries the same 1/h^2, applied
+  // once with the time step; otherwise each derivative is scaled.
+  P.iso = (g.dx == g.dy && g.dx == g.dz) ? 1 : 0;
+  P.dt2 = P.iso ? (g.dt * g.dt) * P.inv_dxx : g.dt * g.dt;
   P.src_x = P.src_y = P.src_z = -1000;
   P.src = 0.f;
   bool fused = false;

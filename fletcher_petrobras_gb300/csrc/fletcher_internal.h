@@ -28,7 +28,8 @@ struct PropParams {
   int ntx, nty, nchunk, chunk, nitems;
   float inv_dx, inv_dy, inv_dz;     // 1/dx, 1/dy, 1/dz
   float inv_dxx, inv_dyy, inv_dzz;  // 1/(dx*dx), 1/(dy*dy), 1/(dz*dz) as the reference forms them
-  float dt2;
+  int iso;                          // dx == dy == dz: derivatives unscaled, dt2 = dt^2 / h^2
+  float dt2;                        // factor of the rhs in the update
   int src_x, src_y, src_z;  // source added to current p,q this step (src_z < 0: none)
   float src;
   int cor_x, cor_y, cor_z;  // last step's source, not stored in the buffer that

@@ -47,14 +47,14 @@ struct Geo {
   static constexpr int OFF_UPD = OFF_ARR + ARR_B;
   static constexpr int OFF_PP = OFF_UPD + UPD_B;
   static constexpr int STAGE_B = (OFF_PP + PP_B + 127) / 128 * 128;
-  static constexpr int DBUF_B = 2 * TY * HX * 8;
+  static constexpr int DBUF_B = 2 * TY * HX * 8;  // D1y rows with their x halo, double-buffered
   static_assert(TY % 4 == 0, "tile rows must be a multiple of 4");
   static_assert(HALO_B % 128 == 0 && ARR_B % 128 == 0 && UPD_B % 128 == 0, "stage regions 128-B aligned");
 };
 
 template <int TY, int S>
 constexpr size_t smem_bytes() {
-  return size_t(S) * Geo<TY>::STAGE_B + Geo<TY>::DBUF_B + 8 * S + 128;
+  return size_t(S) * Geo<TY>::STAGE_B + Geo<TY>::DBUF_B + 8 * S + 8 + 16 + 128;
 }
 
 struct Item {
@@ -75,9 +75,7 @@ __device__ __forceinline__ Item decode_item(int item, const PropParams &P) {
   return it;
 }
 
-__device__ __forceinline__ f2 ldw(const float2 &w) { return *reinterpret_cast<const f2 *>(&w); }
-
-// Thread 0's side of the pipeline: issues the TMA loads of one step.
+// Issues the TMA loads of one step (plane k of item `it`) into `stage`.
 template <int TY>
 __device__ __forceinline__ void issue_step(unsigned char *stage, uint64_t *bar, const Item &it, int k,
                                            const CUtensorMap *tm_cur, const CUtensorMap *tm_prev,
@@ -96,8 +94,7 @@ __device__ __forceinline__ void issue_step(unsigned char *stage, uint64_t *bar, 
 }
 
 // Stencil weights of original/derivatives.h:13-41 (first derivative L1..L4,
-// second derivative K0..K4), as compile-time constants; the 1/d and 1/d^2
-// factors are applied once per derivative.
+// second derivative K0..K4) as compile-time constants.
 constexpr float cL1 = 0.8f, cL2 = -0.2f, cL3 = 0.0380952380952381f, cL4 = -0.0035714285714285713f;
 constexpr float cK0 = -2.84722222222222222222f, cK1 = 1.6f, cK2 = -0.2f, cK3 = 0.02539682539682539682f,
                 cK4 = -0.00178571428571428571f;
@@ -117,9 +114,26 @@ __device__ __forceinline__ f2 d2(f2 c, f2 a1, f2 b1, f2 a2, f2 b2, f2 a3, f2 b3,
   r = fma2(splat(cK3), add2(a3, b3), r);
   return fma2(splat(cK4), add2(a4, b4), r);
 }
+// Applies a spacing factor unless the grid is isotropic (then every factor
+// is folded into one dt^2/h^2 at the end).
+template <bool ISO>
+__device__ __forceinline__ f2 scale(f2 v, float s) {
+  if constexpr (ISO) return v;
+  else return mul2(splat(s), v);
+}
 
-// Next step the producer must load: `ahead` steps after step k of `item`.
-// Returns false when the CTA has no such step.
+// Adds `s` to the register among {c, a[0..3] (offsets +1..+4), b[0..3]
+// (offsets -1..-4)} at offset d from the centre (|d| <= 4).
+__device__ __forceinline__ void add_at(f2 &c, f2 (&a)[4], f2 (&b)[4], int d, f2 s) {
+  if (d == 0) c = add2(c, s);
+#pragma unroll
+  for (int j = 1; j <= 4; ++j) {
+    if (d == j) a[j - 1] = add2(a[j - 1], s);
+    if (d == -j) b[j - 1] = add2(b[j - 1], s);
+  }
+}
+
+// The step `ahead` steps after step k of `item` in this CTA's sequence.
 template <int TY>
 __device__ __forceinline__ bool step_after(const PropParams &P, int item, int k, int ahead, Item &out_it,
                                            int &out_k) {
@@ -137,17 +151,20 @@ __device__ __forceinline__ bool step_after(const PropParams &P, int item, int k,
   return true;
 }
 
-template <int TY, int S, int MINB>
+template <int TY, int S, bool ISO, int MINB>
 __global__ void __launch_bounds__(kTileX *TY, MINB)
     k_propagate_fp32(const __grid_constant__ CUtensorMap tm_cur, const __grid_constant__ CUtensorMap tm_prev,
                      const __grid_constant__ CUtensorMap tm_arr, const __grid_constant__ CUtensorMap tm_upd,
                      const PropParams P) {
   using G = Geo<TY>;
   extern __shared__ unsigned char smem_dyn[];
-  unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_dyn) + 127) & ~uintptr_t(127));
+  // Align in the shared window (pointer arithmetic on the shared array keeps
+  // every access below a shared-memory access).
+  unsigned char *smem = smem_dyn + ((128u - (smem_addr(smem_dyn) & 127u)) & 127u);
   f2 *dbuf = reinterpret_cast<f2 *>(smem + S * G::STAGE_B);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + S * G::STAGE_B + G::DBUF_B);
-  __shared__ int s_abort;
+  uint64_t *xchg = full + S;  // D1y rows written (one arrival per warp)
+  int *s_abort = reinterpret_cast<int *>(xchg + 1);
 
   const int tid = threadIdx.x;
   const int lx = tid & 31;
@@ -156,8 +173,9 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   if (blockIdx.x >= P.nitems) return;
   if (tid == 0) {
     for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
+    mbar_init(xchg, TY);
     mbar_fence_init();
-    s_abort = 0;
+    *s_abort = 0;
     tma_prefetch_desc(&tm_cur);
     tma_prefetch_desc(&tm_prev);
     tma_prefetch_desc(&tm_arr);
@@ -173,8 +191,18 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   }
   __syncthreads();
 
+  // Spacing factors (unused on isotropic grids).
+  const float sx1 = P.inv_dx, sy1 = P.inv_dy, sz1 = P.inv_dz;
+  const float sxx = P.inv_dxx, syy = P.inv_dyy, szz = P.inv_dzz;
+  // Halo-column duty: warps 0 .. TY/4-1 evaluate D1y in the 4 columns left
+  // and right of the tile for all TY rows (lane -> row 4*warp + lane/8).
+  const bool halo_warp = ly < TY / 4;
+  const int hr = ly * 4 + (lx >> 3);
+  const int hxc = (lx & 7) < 4 ? (lx & 7) : G::TX + (lx & 7);
+  const int hh = (hr + kRadius) * G::HX + hxc;
+
   int stage = 0;
-  uint32_t phase = 0;
+  uint32_t phase = 0, xphase = 0;
   int dsel = 0;
   for (int item = blockIdx.x; item < P.nitems; item += gridDim.x) {
     const Item it = decode_item<TY>(item, P);
@@ -183,6 +211,8 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
     const int gx = it.x0 + lx;
     const int gy = it.y0 + ly;
     const bool valid = (gx >= P.bord) && (gx < P.sx - P.bord) && (gy >= P.bord) && (gy < P.sy - P.bord);
+    unsigned long long *out = reinterpret_cast<unsigned long long *>(P.prev) + ((long)gy * P.pitch + gx);
+    const long plane = (long)P.pitch * P.sy;
     const int ci = ly * G::TX + lx;
     const int hc = (ly + kRadius) * G::HX + (lx + kRadius);
 
@@ -195,105 +225,75 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
         if (k >= kend) break;
         unsigned char *st = smem + stage * G::STAGE_B;
         if (!mbar_wait(&full[stage], phase, kWaitLimitNs)) {
-          s_abort = 1;
+          *s_abort = 1;
           atomicOr(P.err, 1u);
+          goto aborted;
         }
         const bool center = (k >= it.z0) && (k < it.z1);
         const bool upd = (k - kRadius >= it.z0);
-
-        // Fused source: add to the (p, q) of the source cell in this CTA's
-        // copy of the plane before any thread reads it.
-        if (k == P.src_z) {
-          const int hx = P.src_x - (it.x0 - kRadius);
-          const int hy = P.src_y - (it.y0 - kRadius);
-          if (hx >= 0 && hx < G::HX && hy >= 0 && hy < G::HY) {
-            __syncthreads();
-            if (tid == 0) {
-              f2 *h = reinterpret_cast<f2 *>(st) + hy * G::HX + hx;
-              *h = add2(*h, splat(P.src));
-            }
-            __syncthreads();
-          }
-        }
-
+        const bool src_plane = (k == P.src_z);
         const f2 *H = reinterpret_cast<const f2 *>(st);
-        const f2 c = H[hc];
-        f2 d1x, d1y, d2x, d2y;
-        {
-          const f2 a1 = H[hc + 1], b1 = H[hc - 1], a2 = H[hc + 2], b2 = H[hc - 2];
-          const f2 a3 = H[hc + 3], b3 = H[hc - 3], a4 = H[hc + 4], b4 = H[hc - 4];
-          d1x = mul2(splat(P.inv_dx), d1(a1, b1, a2, b2, a3, b3, a4, b4));
-          if (center) d2x = mul2(splat(P.inv_dxx), d2(c, a1, b1, a2, b2, a3, b3, a4, b4));
+
+        f2 c = H[hc];
+        f2 xa[4], xb[4], ya[4], yb[4];
+#pragma unroll
+        for (int o = 1; o <= 4; ++o) {
+          xa[o - 1] = H[hc + o];
+          xb[o - 1] = H[hc - o];
+          ya[o - 1] = H[hc + o * G::HX];
+          yb[o - 1] = H[hc - o * G::HX];
         }
-        {
-          constexpr int W = G::HX;
-          const f2 a1 = H[hc + W], b1 = H[hc - W], a2 = H[hc + 2 * W], b2 = H[hc - 2 * W];
-          const f2 a3 = H[hc + 3 * W], b3 = H[hc - 3 * W], a4 = H[hc + 4 * W], b4 = H[hc - 4 * W];
-          d1y = mul2(splat(P.inv_dy), d1(a1, b1, a2, b2, a3, b3, a4, b4));
-          if (center) d2y = mul2(splat(P.inv_dyy), d2(c, a1, b1, a2, b2, a3, b3, a4, b4));
+        // Fused source (original/OpenMP/openmp_insertsource.c:7-13): the
+        // current p and q gain `src` at the source cell before the update
+        // reads them; added to this thread's copies of the plane.
+        if (src_plane) {
+          const f2 sv = splat(P.src);
+          f2 dummy;
+          if (gy == P.src_y && abs(P.src_x - gx) <= kRadius) add_at(c, xa, xb, P.src_x - gx, sv);
+          if (gx == P.src_x && P.src_y != gy && abs(P.src_y - gy) <= kRadius)
+            add_at(dummy, ya, yb, P.src_y - gy, sv);
         }
+        const f2 d1x = scale<ISO>(d1(xa[0], xb[0], xa[1], xb[1], xa[2], xb[2], xa[3], xb[3]), sx1);
+        const f2 d1y = scale<ISO>(d1(ya[0], yb[0], ya[1], yb[1], ya[2], yb[2], ya[3], yb[3]), sy1);
         Pr[j] = c;
         Dx[j] = d1x;
         Dy[j] = d1y;
-
+        f2 d2x, d2y;
         f2 *db = dbuf + dsel * (TY * G::HX);
         if (center) {
+          d2x = scale<ISO>(d2(c, xa[0], xb[0], xa[1], xb[1], xa[2], xb[2], xa[3], xb[3]), sxx);
+          d2y = scale<ISO>(d2(c, ya[0], yb[0], ya[1], yb[1], ya[2], yb[2], ya[3], yb[3]), syy);
           db[ly * G::HX + lx + kRadius] = d1y;
-          if (ly < TY / 4) {
-            // D1y in the 4-column x halo on each side, for DerCross xy.
-            const int r = ly * 4 + (lx >> 3);
-            const int cc = lx & 7;
-            const int hxc = cc < 4 ? cc : G::TX + cc;
-            const int hh = (r + kRadius) * G::HX + hxc;
-            constexpr int W = G::HX;
-            db[r * G::HX + hxc] =
-                mul2(splat(P.inv_dy), d1(H[hh + W], H[hh - W], H[hh + 2 * W], H[hh - 2 * W], H[hh + 3 * W],
-                                         H[hh - 3 * W], H[hh + 4 * W], H[hh - 4 * W]));
-          }
-        }
-        __syncthreads();
-        if (s_abort) {
-          if (tid == 0) {
-            // Drain the loads still in flight (bounded) before leaving.
-            int s2 = stage;
-            uint32_t ph2 = phase;
-            for (int a = 0; a < S - 1; ++a) {
-              Item it2;
-              int k2;
-              if (!step_after<TY>(P, item, k, a, it2, k2)) break;
-              (void)mbar_wait(&full[s2], ph2, kWaitLimitNs);
-              if (++s2 == S) { s2 = 0; ph2 ^= 1u; }
+          if (halo_warp) {
+            f2 ha[4], hb[4];
+#pragma unroll
+            for (int o = 1; o <= 4; ++o) {
+              ha[o - 1] = H[hh + o * G::HX];
+              hb[o - 1] = H[hh - o * G::HX];
             }
-          }
-          return;
-        }
-        if (tid == 0) {
-          // Refill the stage consumed at the previous step (all threads are
-          // past it) with the step S-1 ahead.
-          Item it2;
-          int k2;
-          if (step_after<TY>(P, item, k, S - 1, it2, k2)) {
-            const int s2 = (stage + S - 1) % S;
-            fence_proxy_async_smem();
-            issue_step<TY>(smem + s2 * G::STAGE_B, &full[s2], it2, k2, &tm_cur, &tm_prev, &tm_arr, &tm_upd);
+            if (src_plane) {
+              const int hgy = it.y0 + hr;
+              if (hxc == P.src_x - (it.x0 - kRadius) && P.src_y != hgy && abs(P.src_y - hgy) <= kRadius) {
+                f2 dummy;
+                add_at(dummy, ha, hb, P.src_y - hgy, splat(P.src));
+              }
+            }
+            db[hr * G::HX + hxc] = scale<ISO>(d1(ha[0], hb[0], ha[1], hb[1], ha[2], hb[2], ha[3], hb[3]), sy1);
           }
         }
-        if (center) {
-          const f2 *dr = db + ly * G::HX + lx + kRadius;
-          const f2 dxy = mul2(splat(P.inv_dx), d1(dr[1], dr[-1], dr[2], dr[-2], dr[3], dr[-3], dr[4], dr[-4]));
-          const float *ca = reinterpret_cast<const float *>(st + G::OFF_ARR);
-          const float cxx = ca[ci], cyy = ca[G::NT + ci], cxy = ca[2 * G::NT + ci];
-          A[j] = fma2(splat(cxy), dxy, fma2(splat(cyy), d2y, mul2(splat(cxx), d2x)));
-          B[j] = add2(d2x, d2y);
-        }
+        // Split-phase exchange: announce this warp's D1y (and, by program
+        // order, that it has finished the previous step), update plane k-4,
+        // which needs no exchanged data, then wait for the other warps.
+        __syncwarp();
+        if (lx == 0) mbar_arrive(xchg);
         if (upd) {
           const int cs = (j + 5) % 9;  // ring slot of plane k-4
 #define RP(o) Pr[(cs + (o)) % 9]
 #define RX(o) Dx[(cs + (o)) % 9]
 #define RY(o) Dy[(cs + (o)) % 9]
-          const f2 d2z = mul2(splat(P.inv_dzz), d2(RP(0), RP(1), RP(8), RP(2), RP(7), RP(3), RP(6), RP(4), RP(5)));
-          const f2 dxz = mul2(splat(P.inv_dz), d1(RX(1), RX(8), RX(2), RX(7), RX(3), RX(6), RX(4), RX(5)));
-          const f2 dyz = mul2(splat(P.inv_dz), d1(RY(1), RY(8), RY(2), RY(7), RY(3), RY(6), RY(4), RY(5)));
+          const f2 d2z = scale<ISO>(d2(RP(0), RP(1), RP(8), RP(2), RP(7), RP(3), RP(6), RP(4), RP(5)), szz);
+          const f2 dxz = scale<ISO>(d1(RX(1), RX(8), RX(2), RX(7), RX(3), RX(6), RX(4), RX(5)), sz1);
+          const f2 dyz = scale<ISO>(d1(RY(1), RY(8), RY(2), RY(7), RY(3), RY(6), RY(4), RY(5)), sz1);
 #undef RP
 #undef RX
 #undef RY
@@ -304,16 +304,43 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
           const f2 h1 = fma2(splat(cyz), dyz, fma2(splat(cxz), dxz, fma2(splat(czz), d2z, A[cs])));
           const f2 h2 = sub2(add2(B[cs], d2z), h1);
           const float h1p = lo(h1), h1q = hi(h1), h2p = lo(h2), h2q = hi(h2);
-          const float rhsp = v2px * h2p + v2pz * h1q + v2sz * (h1p - h1q);
-          const float rhsq = v2pn * h2p + v2pz * h1q - v2sz * (h2p - h2q);
+          // Explicit roundings: every unrolled copy computes identical floats.
+          const float t = __fmul_rn(v2pz, h1q);
+          const float rhsp = __fmaf_rn(v2sz, __fsub_rn(h1p, h1q), __fmaf_rn(v2px, h2p, t));
+          const float rhsq = __fmaf_rn(-v2sz, __fsub_rn(h2p, h2q), __fmaf_rn(v2pn, h2p, t));
           f2 old = reinterpret_cast<const f2 *>(st + G::OFF_PP)[ci];
           const int zc = k - kRadius;
-          if (zc == P.cor_z && gx == P.cor_x && gy == P.cor_y) old = add2(old, splat(P.cor));
+          if (zc == P.cor_z) {
+            if (gx == P.cor_x && gy == P.cor_y) old = add2(old, splat(P.cor));
+          }
           const f2 cur = Pr[cs];
           const f2 nw = fma2(mk2(rhsp, rhsq), splat(P.dt2), sub2(add2(cur, cur), old));
-          if (valid) {
-            reinterpret_cast<unsigned long long *>(P.prev)[((long)zc * P.sy + gy) * P.pitch + gx] = nw.v;
+          if (valid) out[(long)zc * plane] = nw.v;
+        }
+        if (!mbar_wait(xchg, xphase, kWaitLimitNs)) {
+          *s_abort = 1;
+          atomicOr(P.err, 2u);
+        }
+        xphase ^= 1u;
+        if (*reinterpret_cast<volatile int *>(s_abort)) goto aborted;
+        if (tid == 0) {
+          // Every warp has arrived for this step, so every thread is past
+          // the previous step: refill its stage with the step S-1 ahead.
+          Item it2;
+          int k2;
+          if (step_after<TY>(P, item, k, S - 1, it2, k2)) {
+            const int s2 = stage == 0 ? S - 1 : stage - 1;
+            fence_proxy_async_smem();
+            issue_step<TY>(smem + s2 * G::STAGE_B, &full[s2], it2, k2, &tm_cur, &tm_prev, &tm_arr, &tm_upd);
           }
+        }
+        if (center) {
+          const f2 *dr = db + ly * G::HX + lx + kRadius;
+          const f2 dxy = scale<ISO>(d1(dr[1], dr[-1], dr[2], dr[-2], dr[3], dr[-3], dr[4], dr[-4]), sx1);
+          const float *ca = reinterpret_cast<const float *>(st + G::OFF_ARR);
+          const float cxx = ca[ci], cyy = ca[G::NT + ci], cxy = ca[2 * G::NT + ci];
+          A[j] = fma2(splat(cxy), dxy, fma2(splat(cyy), d2y, mul2(splat(cxx), d2x)));
+          B[j] = add2(d2x, d2y);
         }
         dsel ^= 1;
         if (++stage == S) {
@@ -323,6 +350,18 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
       }
     }
   }
+  return;
+aborted:
+  // A bounded wait gave up.  Every thread leaves (the others give up on
+  // their own bounded waits or see the flag); thread 0 first waits, bounded,
+  // for the loads that may still be in flight into this CTA's stages.
+  *s_abort = 1;
+  if (tid == 0) {
+    for (int a = 0; a < S - 1; ++a) {
+      const int s2 = (stage + a) % S;
+      (void)mbar_wait(&full[s2], phase ^ uint32_t(stage + a >= S), kWaitLimitNs);
+    }
+  }
 }
 
 // ---- host side ---------------------------------------------------------------
@@ -330,7 +369,8 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
 template <int TY, int S, int MINB>
 static cudaError_t launch_t(const PropLaunch &L, cudaStream_t s) {
   constexpr size_t smem = smem_bytes<TY, S>();
-  auto kern = k_propagate_fp32<TY, S, MINB>;
+  const bool iso = L.p.iso != 0;
+  auto kern = iso ? k_propagate_fp32<TY, S, true, MINB> : k_propagate_fp32<TY, S, false, MINB>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   kern<<<L.grid, kTileX * TY, smem, s>>>(L.cur_halo, L.prev_pt, L.coef_arr, L.coef_upd, L.p);
@@ -339,7 +379,7 @@ static cudaError_t launch_t(const PropLaunch &L, cudaStream_t s) {
 
 // Supported shapes: rows per tile x stages.  TY = 16 runs one 512-thread CTA
 // per SM; TY = 8 runs two 256-thread CTAs per SM.
-#define FLT_SHAPES(X) X(16, 4, 1) X(16, 5, 1) X(16, 3, 1) X(8, 4, 2) X(8, 3, 2) X(12, 4, 1)
+#define FLT_SHAPES(X) X(12, 4, 1) X(12, 5, 1) X(12, 6, 1) X(16, 4, 1) X(8, 4, 2) X(8, 6, 2)
 
 size_t propagate_fp32_smem_bytes(int ty, int st) {
 #define X(a, b, c) \
