@@ -42,15 +42,25 @@ __device__ __forceinline__ uint64_t global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// Waits for phase `parity` of `bar`; gives up after limit_ns nanoseconds and
-// returns false.  Every wait in this library is bounded.
+// Waits for phase `parity` of `bar`; gives up after about limit_ns
+// nanoseconds and returns false.  Every wait in this library is bounded.
+// The clock is read once per 64 failed tries.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint64_t limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_ns();
-  while (!mbar_try_wait(bar, parity)) {
-    if (global_ns() - t0 > limit_ns) return false;
+  for (uint32_t n = 1;; ++n) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((n & 63u) == 0 && global_ns() - t0 > limit_ns) return false;
   }
-  return true;
+}
+// Orders: the values in `v` have been produced (their loads have returned)
+// before any later volatile asm executes.
+__device__ __forceinline__ void consumed(unsigned long long v) { asm volatile("" ::"l"(v)); }
+__device__ __forceinline__ void consumed(float v) { asm volatile("" ::"f"(v)); }
+__device__ __forceinline__ unsigned atom_add_relaxed_cta(unsigned *p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.relaxed.cta.shared::cta.add.u32 %0, [%1], %2;" : "=r"(old) : "r"(smem_addr(p)), "r"(v) : "memory");
+  return old;
 }
 
 // Shared-memory atomic add with acquire-release semantics at CTA scope:

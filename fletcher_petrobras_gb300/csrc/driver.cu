@@ -288,6 +288,7 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   g.tile_rows = rows;
   g.stages = stages;
   g.zchunks = g_req_chunks;
+
   cudaStream_t s = g_stream;
 
   CK(cudaMalloc(&g.F[0], g.npitch * sizeof(float2)));

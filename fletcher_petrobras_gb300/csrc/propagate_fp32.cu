@@ -171,25 +171,36 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   const int ly = tid >> 5;
 
   if (blockIdx.x >= P.nitems) return;
+  // The producer is lane 0 of the last warp (warps 0 .. TY/4-1 carry the
+  // halo-column work).  Its cursor (pr_*) is the next step to load.
+  const bool producer = tid == (TY - 1) * 32;
+  Item pr_it = decode_item<TY>(blockIdx.x, P);
+  int pr_item = blockIdx.x, pr_k = pr_it.z0 - kRadius, pr_stage = 0;
   if (tid == 0) {
     for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
     mbar_init(xchg, TY);
     mbar_fence_init();
     *s_abort = 0;
+  }
+  __syncthreads();
+  if (producer) {
     tma_prefetch_desc(&tm_cur);
     tma_prefetch_desc(&tm_prev);
     tma_prefetch_desc(&tm_arr);
     tma_prefetch_desc(&tm_upd);
     // Prologue: the first S-1 steps of this CTA.
-    const Item i0 = decode_item<TY>(blockIdx.x, P);
-    for (int a = 0; a < S - 1; ++a) {
-      Item it;
-      int k;
-      if (!step_after<TY>(P, blockIdx.x, i0.z0 - kRadius, a, it, k)) break;
-      issue_step<TY>(smem + a * G::STAGE_B, &full[a], it, k, &tm_cur, &tm_prev, &tm_arr, &tm_upd);
+    for (int a = 0; a < S - 1 && pr_item < P.nitems; ++a) {
+      issue_step<TY>(smem + pr_stage * G::STAGE_B, &full[pr_stage], pr_it, pr_k, &tm_cur, &tm_prev, &tm_arr, &tm_upd);
+      if (++pr_stage == S) pr_stage = 0;
+      if (++pr_k >= pr_it.z1 + kRadius) {
+        pr_item += gridDim.x;
+        if (pr_item < P.nitems) {
+          pr_it = decode_item<TY>(pr_item, P);
+          pr_k = pr_it.z0 - kRadius;
+        }
+      }
     }
   }
-  __syncthreads();
 
   // Spacing factors (unused on isotropic grids).
   const float sx1 = P.inv_dx, sy1 = P.inv_dy, sz1 = P.inv_dz;
@@ -323,15 +334,19 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
         }
         xphase ^= 1u;
         if (*reinterpret_cast<volatile int *>(s_abort)) goto aborted;
-        if (tid == 0) {
-          // Every warp has arrived for this step, so every thread is past
-          // the previous step: refill its stage with the step S-1 ahead.
-          Item it2;
-          int k2;
-          if (step_after<TY>(P, item, k, S - 1, it2, k2)) {
-            const int s2 = stage == 0 ? S - 1 : stage - 1;
-            fence_proxy_async_smem();
-            issue_step<TY>(smem + s2 * G::STAGE_B, &full[s2], it2, k2, &tm_cur, &tm_prev, &tm_arr, &tm_upd);
+        // Every warp has arrived for this step, so every thread is past the
+        // previous step: refill that step's stage with the next step due.
+        if (producer && pr_item < P.nitems) {
+          fence_proxy_async_smem();
+          issue_step<TY>(smem + pr_stage * G::STAGE_B, &full[pr_stage], pr_it, pr_k, &tm_cur, &tm_prev, &tm_arr,
+                         &tm_upd);
+          if (++pr_stage == S) pr_stage = 0;
+          if (++pr_k >= pr_it.z1 + kRadius) {
+            pr_item += gridDim.x;
+            if (pr_item < P.nitems) {
+              pr_it = decode_item<TY>(pr_item, P);
+              pr_k = pr_it.z0 - kRadius;
+            }
           }
         }
         if (center) {
@@ -368,8 +383,8 @@ aborted:
 
 template <int TY, int S, int MINB>
 static cudaError_t launch_t(const PropLaunch &L, cudaStream_t s) {
-  constexpr size_t smem = smem_bytes<TY, S>();
   const bool iso = L.p.iso != 0;
+  constexpr size_t smem = smem_bytes<TY, S>();
   auto kern = iso ? k_propagate_fp32<TY, S, true, MINB> : k_propagate_fp32<TY, S, false, MINB>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -379,7 +394,7 @@ static cudaError_t launch_t(const PropLaunch &L, cudaStream_t s) {
 
 // Supported shapes: rows per tile x stages.  TY = 16 runs one 512-thread CTA
 // per SM; TY = 8 runs two 256-thread CTAs per SM.
-#define FLT_SHAPES(X) X(12, 4, 1) X(12, 5, 1) X(12, 6, 1) X(16, 4, 1) X(8, 4, 2) X(8, 6, 2)
+#define FLT_SHAPES(X) X(12, 4, 1) X(12, 5, 1) X(12, 6, 1) X(16, 4, 1) X(8, 4, 2)
 
 size_t propagate_fp32_smem_bytes(int ty, int st) {
 #define X(a, b, c) \
