@@ -34,6 +34,7 @@ SIGNATURES = {
     "FLETCHER_KernelLaunches": (C.c_long, []),
     "FLETCHER_DeviceBytes": (C.c_size_t, []),
     "FLETCHER_BytesPerCell": (C.c_double, []),
+    "FLETCHER_ReadFieldNoAlloc": (C.c_int, [C.c_void_p] + [C.c_int] * 5 + [FP]),
     "FLETCHER_ModelHomogeneous": (None, [C.c_long] + [C.c_float] * 6 + [FP]),
     "FLETCHER_ModelLayered": (None, [C.c_int] * 6 + [C.c_uint64] + [C.c_float] * 3 + [FP, IP]),
     "FLETCHER_RandomVelocityBoundary": (None, [C.c_int] * 8 + [FP, FP, C.c_uint]),

@@ -70,6 +70,14 @@ int fail(int code, const char *fmt, ...) {
   return code;
 }
 
+}  // namespace
+
+// Error reporting for other translation units of this library (same sticky
+// status and error mode as the DRIVER_* entry points).
+int flt_record_error(int code, const char *msg) { return fail(code, "%s", msg); }
+
+namespace {
+
 #define CK(call)                                                                                   \
   do {                                                                                             \
     cudaError_t e_ = (call);                                                                       \

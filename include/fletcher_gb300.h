@@ -118,6 +118,25 @@ size_t FLETCHER_DeviceBytes(void);
  * next field). */
 double FLETCHER_BytesPerCell(void);
 
+/* No counterpart in the reference.  Read-back for callers that cannot
+ * allocate device memory: codes that reserve the whole GPU for their own
+ * wavefield and coefficient volumes up front, or whose time loop must not
+ * call cudaMalloc (an allocation there fails once memory is fully reserved,
+ * or stalls the stream).  Copies component `comp` (0 = p, 1 = q) of a
+ * caller-owned (p, q) pair volume on the current device -- float pairs,
+ * [sz][sy][pitch], x fastest, pitch >= sx, the layout of this library's own
+ * field buffers -- into host_out (sx*sy*sz floats).  It allocates nothing:
+ * it stages through a fixed array of FLETCHER_NOALLOC_MAX_CELLS floats
+ * (16 MiB) built into the library, which every GPU that loads the library
+ * holds until the process exits; larger grids are rejected with
+ * FLETCHER_ERR_ARGS.  The first call on a device looks up that array's
+ * device address, so make it before any stream capture.  Calls share the
+ * array: calls that overlap on the GPU race.  Runs on FLETCHER_GetStream()
+ * and returns when host_out is filled; returns a FLETCHER_* status. */
+#define FLETCHER_NOALLOC_MAX_CELLS (4u * 1024u * 1024u)
+int FLETCHER_ReadFieldNoAlloc(const void *dev_pairs, int sx, int sy, int sz, int pitch, int comp,
+                              float *host_out);
+
 /* ===== Part 3: host-side model preparation and time loop ================= */
 
 /* Fills the six model arrays (vpz vsv epsilon delta phi theta, n floats

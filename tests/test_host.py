@@ -83,6 +83,7 @@ def test_problem_geometry():
 def header_functions():
     txt = open(os.path.join(ROOT, "include", "fletcher_gb300.h")).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    txt = "\n".join(line for line in txt.splitlines() if not line.lstrip().startswith("#"))
     return sorted(set(re.findall(r"\b((?:DRIVER|FLETCHER)_[A-Za-z_]+)\s*\(", txt)))
 
 
