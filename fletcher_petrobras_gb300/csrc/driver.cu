@@ -43,7 +43,7 @@ struct State {
   Source pending;      // registered by DRIVER_InsertSource, applied by the next step
   Source owed;         // source of the last step, missing from the previous-field buffer
   CUtensorMap halo[2], pt[2], arr, upd;
-  int tile_rows = 12, stages = 4, zchunks = 0;
+  int tile_rows = 12, stages = 5, zchunks = 0;
   int grid = 0, nitems = 0, ntx = 0, nty = 0, nchunk = 0, chunk = 0;
   long launches = 0;
   size_t dev_bytes = 0;
@@ -280,7 +280,7 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
     return fail(FLETCHER_ERR_ARGS, "model arrays must not be NULL");
   if (g_form != FLETCHER_FORM_FP32) return fail(FLETCHER_ERR_ARGS, "unknown storage form %d", g_form);
   const int rows = g_req_rows ? g_req_rows : 12;
-  const int stages = g_req_stages ? g_req_stages : 4;
+  const int stages = g_req_stages ? g_req_stages : 5;
   if (!propagate_fp32_supported(rows, stages))
     return fail(FLETCHER_ERR_ARGS, "tile shape (%d rows, %d stages) is not built", rows, stages);
   if (ensure_stream()) return g_last_err;
@@ -530,7 +530,7 @@ extern "C" int FLETCHER_SetForm(int form) {
 }
 
 extern "C" int FLETCHER_SetTileConfig(int rows, int stages, int zchunks) {
-  const int r = rows ? rows : 12, s = stages ? stages : 4;
+  const int r = rows ? rows : 12, s = stages ? stages : 5;
   if (!propagate_fp32_supported(r, s)) return fail(FLETCHER_ERR_ARGS, "tile shape (%d, %d) is not built", r, s);
   if (zchunks < 0) return fail(FLETCHER_ERR_ARGS, "zchunks must be >= 0");
   g_req_rows = rows;

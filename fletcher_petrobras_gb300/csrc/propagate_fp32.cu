@@ -188,8 +188,8 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
     tma_prefetch_desc(&tm_prev);
     tma_prefetch_desc(&tm_arr);
     tma_prefetch_desc(&tm_upd);
-    // Prologue: the first S-1 steps of this CTA.
-    for (int a = 0; a < S - 1 && pr_item < P.nitems; ++a) {
+    // Prologue: the first S-2 steps of this CTA.
+    for (int a = 0; a < S - 2 && pr_item < P.nitems; ++a) {
       issue_step<TY>(smem + pr_stage * G::STAGE_B, &full[pr_stage], pr_it, pr_k, &tm_cur, &tm_prev, &tm_arr, &tm_upd);
       if (++pr_stage == S) pr_stage = 0;
       if (++pr_k >= pr_it.z1 + kRadius) {
@@ -297,6 +297,22 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
         // which needs no exchanged data, then wait for the other warps.
         __syncwarp();
         if (lx == 0) mbar_arrive(xchg);
+        // The producer has passed the exchange of the previous step, so every
+        // thread is past the step before it: refill that step's stage with
+        // the next step due (S-2 steps ahead of this one).
+        if (producer && pr_item < P.nitems) {
+          fence_proxy_async_smem();
+          issue_step<TY>(smem + pr_stage * G::STAGE_B, &full[pr_stage], pr_it, pr_k, &tm_cur, &tm_prev, &tm_arr,
+                         &tm_upd);
+          if (++pr_stage == S) pr_stage = 0;
+          if (++pr_k >= pr_it.z1 + kRadius) {
+            pr_item += gridDim.x;
+            if (pr_item < P.nitems) {
+              pr_it = decode_item<TY>(pr_item, P);
+              pr_k = pr_it.z0 - kRadius;
+            }
+          }
+        }
         if (upd) {
           const int cs = (j + 5) % 9;  // ring slot of plane k-4
 #define RP(o) Pr[(cs + (o)) % 9]
@@ -333,22 +349,6 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
           atomicOr(P.err, 2u);
         }
         xphase ^= 1u;
-        if (*reinterpret_cast<volatile int *>(s_abort)) goto aborted;
-        // Every warp has arrived for this step, so every thread is past the
-        // previous step: refill that step's stage with the next step due.
-        if (producer && pr_item < P.nitems) {
-          fence_proxy_async_smem();
-          issue_step<TY>(smem + pr_stage * G::STAGE_B, &full[pr_stage], pr_it, pr_k, &tm_cur, &tm_prev, &tm_arr,
-                         &tm_upd);
-          if (++pr_stage == S) pr_stage = 0;
-          if (++pr_k >= pr_it.z1 + kRadius) {
-            pr_item += gridDim.x;
-            if (pr_item < P.nitems) {
-              pr_it = decode_item<TY>(pr_item, P);
-              pr_k = pr_it.z0 - kRadius;
-            }
-          }
-        }
         if (center) {
           const f2 *dr = db + ly * G::HX + lx + kRadius;
           const f2 dxy = scale<ISO>(d1(dr[1], dr[-1], dr[2], dr[-2], dr[3], dr[-3], dr[4], dr[-4]), sx1);
@@ -372,7 +372,7 @@ aborted:
   // for the loads that may still be in flight into this CTA's stages.
   *s_abort = 1;
   if (tid == 0) {
-    for (int a = 0; a < S - 1; ++a) {
+    for (int a = 0; a < S - 2; ++a) {
       const int s2 = (stage + a) % S;
       (void)mbar_wait(&full[s2], phase ^ uint32_t(stage + a >= S), kWaitLimitNs);
     }
@@ -394,7 +394,7 @@ static cudaError_t launch_t(const PropLaunch &L, cudaStream_t s) {
 
 // Supported shapes: rows per tile x stages.  TY = 16 runs one 512-thread CTA
 // per SM; TY = 8 runs two 256-thread CTAs per SM.
-#define FLT_SHAPES(X) X(12, 4, 1) X(12, 5, 1) X(12, 6, 1) X(16, 4, 1) X(8, 4, 2)
+#define FLT_SHAPES(X) X(12, 4, 1) X(12, 5, 1) X(12, 6, 1) X(16, 5, 1) X(8, 5, 2)
 
 size_t propagate_fp32_smem_bytes(int ty, int st) {
 #define X(a, b, c) \

@@ -379,3 +379,30 @@ float orc_recommended_dt(long n, const float *vpz, const float *epsilon, float d
 
 /* Host threads the OpenMP loops use. */
 int orc_threads(void) { return omp_get_max_threads(); }
+
+/* ---- FP16-storage emulation -------------------------------------------
+ * The reduced-precision form stores p and q as FP16 with one power-of-two
+ * scale per z-plane (per field buffer) and does all arithmetic in FP32.
+ * `orc_quantize_planes` rounds a field to that storage (round to nearest
+ * even, scale 2^k chosen so the plane's largest magnitude lands in
+ * [2^13, 2^14)), in place, returning the values the kernel would read.
+ * Used by the tests to bound the storage error against the FP64 oracle. */
+static float q16(float v, float scale, float inv) {
+  _Float16 h = (_Float16)(v * scale);
+  return (float)h * inv;
+}
+
+void orc_quantize_planes(int sx, int sy, int sz, float *f) {
+  const long plane = (long)sx * sy;
+#pragma omp parallel for schedule(static)
+  for (int z = 0; z < sz; z++) {
+    float m = 0.0f;
+    for (long i = z * plane; i < (z + 1) * plane; i++) m = fmaxf(m, fabsf(f[i]));
+    if (m == 0.0f) continue;
+    int e;
+    frexpf(m, &e); /* m in [2^(e-1), 2^e) */
+    if (e < -100) e = -100; /* keep 2^(14-e) finite; such planes round to zero */
+    const float scale = ldexpf(1.0f, 14 - e), inv = ldexpf(1.0f, e - 14);
+    for (long i = z * plane; i < (z + 1) * plane; i++) f[i] = q16(f[i], scale, inv);
+  }
+}
