@@ -42,7 +42,8 @@ struct State {
   int cur = 0;
   Source pending;      // registered by DRIVER_InsertSource, applied by the next step
   Source owed;         // source of the last step, missing from the previous-field buffer
-  CUtensorMap halo[2], pt[2], arr, upd;
+  ShotDesc desc;                 // the shot (passed by value to every launch)
+  ShotMaps maps;                 // its TMA descriptors
   int tile_rows = 12, stages = 5, zchunks = 0;
   int grid = 0, nitems = 0, ntx = 0, nty = 0, nchunk = 0, chunk = 0;
   long launches = 0;
@@ -268,6 +269,45 @@ int ensure_stream() {
   return FLETCHER_OK;
 }
 
+}  // namespace
+
+namespace flt {
+
+// The six TMA descriptors of one shot: both field buffers with the halo box
+// and the point box, and the coefficient block with the 3- and 7-coefficient
+// boxes.
+int build_maps(ShotMaps *m, float2 *const F[2], float *coef, int sx, int sy, int sz, int pitch, int TY) {
+  const cuuint64_t dims[3] = {(cuuint64_t)sx, (cuuint64_t)sy, (cuuint64_t)sz};
+  const cuuint64_t str[2] = {(cuuint64_t)pitch * 8, (cuuint64_t)pitch * sy * 8};
+  const cuuint32_t hbox[3] = {(cuuint32_t)(kTileX + 2 * kRadius), (cuuint32_t)(TY + 2 * kRadius), 1};
+  const cuuint32_t pbox[3] = {(cuuint32_t)kTileX, (cuuint32_t)TY, 1};
+  for (int b = 0; b < 2; ++b) {
+    if (encode(&m->halo[b], CU_TENSOR_MAP_DATA_TYPE_INT64, 3, F[b], dims, str, hbox)) return g_last_err;
+    if (encode(&m->pt[b], CU_TENSOR_MAP_DATA_TYPE_INT64, 3, F[b], dims, str, pbox)) return g_last_err;
+  }
+  const cuuint64_t cdims[4] = {(cuuint64_t)sx, (cuuint64_t)sy, (cuuint64_t)kNumCoef, (cuuint64_t)sz};
+  const cuuint64_t cstr[3] = {(cuuint64_t)pitch * 4, (cuuint64_t)pitch * sy * 4,
+                              (cuuint64_t)pitch * sy * kNumCoef * 4};
+  const cuuint32_t abox[4] = {(cuuint32_t)kTileX, (cuuint32_t)TY, (cuuint32_t)kArrivalCoef, 1};
+  const cuuint32_t ubox[4] = {(cuuint32_t)kTileX, (cuuint32_t)TY, (cuuint32_t)kUpdateCoef, 1};
+  if (encode(&m->arr, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, coef, cdims, cstr, abox)) return g_last_err;
+  if (encode(&m->upd, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, coef, cdims, cstr, ubox)) return g_last_err;
+  return FLETCHER_OK;
+}
+
+// Work items of one shot, chunk-major then rows then columns, so CTAs that
+// run at the same time work on neighbouring tiles of the same z range.
+void fill_items(int4 *items, int shot, int ntx, int nty, int nchunk, int TY) {
+  int n = 0;
+  for (int c = 0; c < nchunk; ++c)
+    for (int ty = 0; ty < nty; ++ty)
+      for (int tx = 0; tx < ntx; ++tx) items[n++] = make_int4(shot, kRadius + tx * kTileX, kRadius + ty * TY, c);
+}
+
+}  // namespace flt
+
+namespace {
+
 int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, float dt, const float *vpz,
                const float *vsv, const float *epsilon, const float *delta, const float *phi, const float *theta,
                const float *pp, const float *pc, const float *qp, const float *qc) {
@@ -333,32 +373,22 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   CK(cudaStreamSynchronize(s));
   CK(cudaFree(raw));
 
-  // Tensor maps.
+  // Tensor maps and the shot descriptor.
   const int TY = rows;
-  {
-    const cuuint64_t dims[3] = {(cuuint64_t)sx, (cuuint64_t)sy, (cuuint64_t)sz};
-    const cuuint64_t str[2] = {(cuuint64_t)g.pitch * 8, (cuuint64_t)g.pitch * sy * 8};
-    const cuuint32_t hbox[3] = {(cuuint32_t)(kTileX + 2 * kRadius), (cuuint32_t)(TY + 2 * kRadius), 1};
-    const cuuint32_t pbox[3] = {(cuuint32_t)kTileX, (cuuint32_t)TY, 1};
-    for (int b = 0; b < 2; ++b) {
-      if (encode(&g.halo[b], CU_TENSOR_MAP_DATA_TYPE_INT64, 3, g.F[b], dims, str, hbox)) return g_last_err;
-      if (encode(&g.pt[b], CU_TENSOR_MAP_DATA_TYPE_INT64, 3, g.F[b], dims, str, pbox)) return g_last_err;
-    }
-    const cuuint64_t cdims[4] = {(cuuint64_t)sx, (cuuint64_t)sy, (cuuint64_t)kNumCoef, (cuuint64_t)sz};
-    const cuuint64_t cstr[3] = {(cuuint64_t)g.pitch * 4, (cuuint64_t)g.pitch * sy * 4,
-                                (cuuint64_t)g.pitch * sy * kNumCoef * 4};
-    const cuuint32_t abox[4] = {(cuuint32_t)kTileX, (cuuint32_t)TY, (cuuint32_t)kArrivalCoef, 1};
-    const cuuint32_t ubox[4] = {(cuuint32_t)kTileX, (cuuint32_t)TY, (cuuint32_t)kUpdateCoef, 1};
-    if (encode(&g.arr, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, g.coef, cdims, cstr, abox)) return g_last_err;
-    if (encode(&g.upd, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, g.coef, cdims, cstr, ubox)) return g_last_err;
-  }
-  // Work decomposition.
+  if (build_maps(&g.maps, g.F, g.coef, sx, sy, sz, g.pitch, TY)) return g_last_err;
   g.ntx = (sx - bord - kRadius + kTileX - 1) / kTileX;
   g.nty = (sy - bord - kRadius + TY - 1) / TY;
   const int ctas = g.num_sms * propagate_fp32_ctas_per_sm(TY);
   choose_chunks(ctas, g.ntx * g.nty, sz - 2 * bord, g.zchunks, &g.nchunk, &g.chunk);
   g.nitems = g.ntx * g.nty * g.nchunk;
   g.grid = g.nitems < ctas ? g.nitems : ctas;
+  memset(&g.desc, 0, sizeof(g.desc));
+  g.desc.F[0] = g.F[0];
+  g.desc.F[1] = g.F[1];
+  g.desc.sx = sx; g.desc.sy = sy; g.desc.sz = sz; g.desc.pitch = g.pitch; g.desc.bord = bord;
+  g.desc.ntx = g.ntx; g.desc.nty = g.nty; g.desc.chunk = g.chunk;
+  g.desc.src_x = g.desc.src_y = g.desc.src_z = -1000;
+  g.desc.cor_x = g.desc.cor_y = g.desc.cor_z = -1000;
   g.launches = 0;
   g.pending = Source();
   g.owed = Source();
@@ -370,17 +400,20 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
 int step() {
   PropLaunch L;
   const int c = g.cur, p = 1 - g.cur;
-  L.cur_halo = g.halo[c];
-  L.prev_pt = g.pt[p];
-  L.coef_arr = g.arr;
-  L.coef_upd = g.upd;
   L.tile_rows = g.tile_rows;
   L.stages = g.stages;
   L.grid = g.grid;
+  L.batch = false;
+  L.m.cur_halo = g.maps.halo[c];
+  L.m.prev_pt = g.maps.pt[p];
+  L.m.arr = g.maps.arr;
+  L.m.upd = g.maps.upd;
   PropParams &P = L.p;
-  P.prev = g.F[p];
-  P.sx = g.sx; P.sy = g.sy; P.sz = g.sz; P.pitch = g.pitch; P.bord = g.bord;
-  P.ntx = g.ntx; P.nty = g.nty; P.nchunk = g.nchunk; P.chunk = g.chunk; P.nitems = g.nitems;
+  P.shots = nullptr;
+  P.maps = nullptr;
+  P.items = nullptr;
+  P.nitems = g.nitems;
+  P.parity = c;
   P.inv_dx = 1.0f / g.dx;
   P.inv_dy = 1.0f / g.dy;
   P.inv_dz = 1.0f / g.dz;
@@ -391,15 +424,20 @@ int step() {
   // once with the time step; otherwise each derivative is scaled.
   P.iso = (g.dx == g.dy && g.dx == g.dz) ? 1 : 0;
   P.dt2 = P.iso ? (g.dt * g.dt) * P.inv_dxx : g.dt * g.dt;
-  P.src_x = P.src_y = P.src_z = -1000;
+  P.err = g.err_dev;
+  ShotDesc &want = P.one;
+  want = g.desc;
+  want.src_x = want.src_y = want.src_z = -1000;
+  want.cor_x = want.cor_y = want.cor_z = -1000;
   P.src = 0.f;
+  P.cor = 0.f;
   bool fused = false;
   if (g.pending.on) {
     if (in_update_region(g.pending.idx)) {
       const long i = g.pending.idx;
-      P.src_x = (int)(i % g.sx);
-      P.src_y = (int)((i / g.sx) % g.sy);
-      P.src_z = (int)(i / ((long)g.sx * g.sy));
+      want.src_x = (int)(i % g.sx);
+      want.src_y = (int)((i / g.sx) % g.sy);
+      want.src_z = (int)(i / ((long)g.sx * g.sy));
       P.src = g.pending.val;
       fused = true;
     } else {
@@ -407,16 +445,13 @@ int step() {
       CK(cudaGetLastError());
     }
   }
-  P.cor_x = P.cor_y = P.cor_z = -1000;
-  P.cor = 0.f;
   if (g.owed.on) {
     const long i = g.owed.idx;
-    P.cor_x = (int)(i % g.sx);
-    P.cor_y = (int)((i / g.sx) % g.sy);
-    P.cor_z = (int)(i / ((long)g.sx * g.sy));
+    want.cor_x = (int)(i % g.sx);
+    want.cor_y = (int)((i / g.sx) % g.sy);
+    want.cor_z = (int)(i / ((long)g.sx * g.sy));
     P.cor = g.owed.val;
   }
-  P.err = g.err_dev;
   CK(propagate_fp32_launch(L, g_stream));
   ++g.launches;
   // The buffer that was current becomes the previous field; it lacks the

@@ -20,29 +20,53 @@ enum DevCoef {
 constexpr int kArrivalCoef = 3;
 constexpr int kUpdateCoef = 7;
 
-// One plain FP32 step.  The fields are stored as (p, q) pairs of float,
-// [z][y][pitch] with x fastest.
-struct PropParams {
-  float2 *prev;             // pp/qp pairs: read through TMA, written in place
+// One shot's geometry and buffers, in device memory (read by every launch).
+// The fields are stored as (p, q) pairs of float, [z][y][pitch] with x fastest.
+struct ShotDesc {
+  float2 *F[2];                  // the two field buffers
   int sx, sy, sz, pitch, bord;
-  int ntx, nty, nchunk, chunk, nitems;
+  int ntx, nty, chunk;           // tiles in x and y, z-chunk length
+  int src_x, src_y, src_z;       // cell that gains the step's source (src_z < 0: none)
+  int cor_x, cor_y, cor_z;       // cell whose previous-field value lacks the last step's
+                                 //   source (added on read; cor_z < 0: none)
+  int pad[2];
+};
+
+// TMA descriptors of one shot (64-byte aligned in device memory).
+struct alignas(64) ShotMaps {
+  CUtensorMap halo[2];  // field buffer b, box (TX+8, TY+8, 1)
+  CUtensorMap pt[2];    // field buffer b, box (TX, TY, 1)
+  CUtensorMap arr;      // coefficients, box (TX, TY, 3, 1)
+  CUtensorMap upd;      // coefficients, box (TX, TY, 7, 1)
+};
+
+// One launch: every active shot advances one step.  Work items are
+// {shot, x0, y0, chunk index}, ordered by shot.
+struct PropParams {
+  ShotDesc one;                     // single-shot launches: the shot itself
+  const ShotDesc *shots;            // batched launches: per-shot descriptors
+  const ShotMaps *maps;
+  const int4 *items;
+  int nitems;
+  int parity;                       // current field = F[parity], previous = F[1 - parity]
   float inv_dx, inv_dy, inv_dz;     // 1/dx, 1/dy, 1/dz
   float inv_dxx, inv_dyy, inv_dzz;  // 1/(dx*dx), 1/(dy*dy), 1/(dz*dz) as the reference forms them
   int iso;                          // dx == dy == dz: derivatives unscaled, dt2 = dt^2 / h^2
   float dt2;                        // factor of the rhs in the update
-  int src_x, src_y, src_z;  // source added to current p,q this step (src_z < 0: none)
-  float src;
-  int cor_x, cor_y, cor_z;  // last step's source, not stored in the buffer that
-  float cor;                //   is now the previous field: added on read
-  unsigned int *err;        // error word (bit 0: bounded wait gave up)
+  float src;                        // value added at each shot's source cell (src_z >= 0)
+  float cor;                        // value owed at each shot's cor cell (cor_z >= 0)
+  unsigned int *err;                // error word (bit 0: bounded wait gave up)
+};
+
+// The four descriptors a single-shot launch passes as kernel parameters.
+struct SingleMaps {
+  CUtensorMap cur_halo, prev_pt, arr, upd;
 };
 
 struct PropLaunch {
-  CUtensorMap cur_halo;   // current pairs, box (TX+8, TY+8, 1)
-  CUtensorMap prev_pt;    // previous pairs, box (TX, TY, 1)
-  CUtensorMap coef_arr;   // coefficients, box (TX, TY, 3, 1)
-  CUtensorMap coef_upd;   // coefficients, box (TX, TY, 7, 1)
   PropParams p;
+  SingleMaps m;           // single-shot launches
+  bool batch;             // true: p.shots / p.maps / p.items describe the work
   int tile_rows;          // TY
   int stages;
   int grid;

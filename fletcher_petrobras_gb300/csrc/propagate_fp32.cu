@@ -57,39 +57,58 @@ constexpr size_t smem_bytes() {
   return size_t(S) * Geo<TY>::STAGE_B + Geo<TY>::DBUF_B + 8 * S + 8 + 16 + 128;
 }
 
+// A work item resolved against its shot: tile origin, z range, and (batched
+// launches) the shot's descriptors.
 struct Item {
   int x0, y0, z0, z1;
+  int shot;
 };
 
-template <int TY>
+template <int TY, bool BATCH>
 __device__ __forceinline__ Item decode_item(int item, const PropParams &P) {
   Item it;
-  const int tx = item % P.ntx;
-  const int r = item / P.ntx;
-  const int ty = r % P.nty;
-  const int ch = r / P.nty;
-  it.x0 = kRadius + tx * kTileX;
-  it.y0 = kRadius + ty * TY;
-  it.z0 = P.bord + ch * P.chunk;
-  it.z1 = min(it.z0 + P.chunk, P.sz - P.bord);
+  if constexpr (BATCH) {
+    const int4 w = P.items[item];  // {shot, x0, y0, chunk index}
+    const ShotDesc &d = P.shots[w.x];
+    it.x0 = w.y;
+    it.y0 = w.z;
+    it.z0 = d.bord + w.w * d.chunk;
+    it.z1 = min(it.z0 + d.chunk, d.sz - d.bord);
+    it.shot = w.x;
+  } else {
+    const ShotDesc &d = P.one;
+    const int tx = item % d.ntx;
+    const int r = item / d.ntx;
+    const int ty = r % d.nty;
+    const int ch = r / d.nty;
+    it.x0 = kRadius + tx * kTileX;
+    it.y0 = kRadius + ty * TY;
+    it.z0 = d.bord + ch * d.chunk;
+    it.z1 = min(it.z0 + d.chunk, d.sz - d.bord);
+    it.shot = 0;
+  }
   return it;
 }
+
+// Descriptors used for one step of item `it`.
+struct StepMaps {
+  const CUtensorMap *cur, *prev, *arr, *upd;
+};
 
 // Issues the TMA loads of one step (plane k of item `it`) into `stage`.
 template <int TY>
 __device__ __forceinline__ void issue_step(unsigned char *stage, uint64_t *bar, const Item &it, int k,
-                                           const CUtensorMap *tm_cur, const CUtensorMap *tm_prev,
-                                           const CUtensorMap *tm_arr, const CUtensorMap *tm_upd) {
+                                           const StepMaps &m) {
   using G = Geo<TY>;
   const bool center = (k >= it.z0) && (k < it.z1);
   const bool upd = (k - kRadius >= it.z0);
   const uint32_t bytes = G::HALO_B + (center ? G::ARR_B : 0) + (upd ? G::UPD_B + G::PP_B : 0);
   mbar_arrive_expect_tx(bar, bytes);
-  tma_load_3d(stage, tm_cur, bar, it.x0 - kRadius, it.y0 - kRadius, k);
-  if (center) tma_load_4d(stage + G::OFF_ARR, tm_arr, bar, it.x0, it.y0, 0, k);
+  tma_load_3d(stage, m.cur, bar, it.x0 - kRadius, it.y0 - kRadius, k);
+  if (center) tma_load_4d(stage + G::OFF_ARR, m.arr, bar, it.x0, it.y0, 0, k);
   if (upd) {
-    tma_load_4d(stage + G::OFF_UPD, tm_upd, bar, it.x0, it.y0, kArrivalCoef, k - kRadius);
-    tma_load_3d(stage + G::OFF_PP, tm_prev, bar, it.x0, it.y0, k - kRadius);
+    tma_load_4d(stage + G::OFF_UPD, m.upd, bar, it.x0, it.y0, kArrivalCoef, k - kRadius);
+    tma_load_3d(stage + G::OFF_PP, m.prev, bar, it.x0, it.y0, k - kRadius);
   }
 }
 
@@ -134,16 +153,16 @@ __device__ __forceinline__ void add_at(f2 &c, f2 (&a)[4], f2 (&b)[4], int d, f2 
 }
 
 // The step `ahead` steps after step k of `item` in this CTA's sequence.
-template <int TY>
+template <int TY, bool BATCH>
 __device__ __forceinline__ bool step_after(const PropParams &P, int item, int k, int ahead, Item &out_it,
                                            int &out_k) {
-  Item it = decode_item<TY>(item, P);
+  Item it = decode_item<TY, BATCH>(item, P);
   int kk = k + ahead;
   while (kk >= it.z1 + kRadius) {
     const int over = kk - (it.z1 + kRadius);
     item += gridDim.x;
     if (item >= P.nitems) return false;
-    it = decode_item<TY>(item, P);
+    it = decode_item<TY, BATCH>(item, P);
     kk = it.z0 - kRadius + over;
   }
   out_it = it;
@@ -151,11 +170,9 @@ __device__ __forceinline__ bool step_after(const PropParams &P, int item, int k,
   return true;
 }
 
-template <int TY, int S, bool ISO, int MINB>
+template <int TY, int S, bool ISO, bool BATCH, int MINB>
 __global__ void __launch_bounds__(kTileX *TY, MINB)
-    k_propagate_fp32(const __grid_constant__ CUtensorMap tm_cur, const __grid_constant__ CUtensorMap tm_prev,
-                     const __grid_constant__ CUtensorMap tm_arr, const __grid_constant__ CUtensorMap tm_upd,
-                     const PropParams P) {
+    k_propagate_fp32(const __grid_constant__ SingleMaps SM, const __grid_constant__ PropParams P) {
   using G = Geo<TY>;
   extern __shared__ unsigned char smem_dyn[];
   // Align in the shared window (pointer arithmetic on the shared array keeps
@@ -174,7 +191,23 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   // The producer is lane 0 of the last warp (warps 0 .. TY/4-1 carry the
   // halo-column work).  Its cursor (pr_*) is the next step to load.
   const bool producer = tid == (TY - 1) * 32;
-  Item pr_it = decode_item<TY>(blockIdx.x, P);
+  auto maps_of = [&](const Item &it) {
+    StepMaps m;
+    if constexpr (BATCH) {
+      const ShotMaps *sm = P.maps + it.shot;
+      m.cur = &sm->halo[P.parity];
+      m.prev = &sm->pt[P.parity ^ 1];
+      m.arr = &sm->arr;
+      m.upd = &sm->upd;
+    } else {
+      m.cur = &SM.cur_halo;
+      m.prev = &SM.prev_pt;
+      m.arr = &SM.arr;
+      m.upd = &SM.upd;
+    }
+    return m;
+  };
+  Item pr_it = decode_item<TY, BATCH>(blockIdx.x, P);
   int pr_item = blockIdx.x, pr_k = pr_it.z0 - kRadius, pr_stage = 0;
   if (tid == 0) {
     for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
@@ -184,18 +217,21 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   }
   __syncthreads();
   if (producer) {
-    tma_prefetch_desc(&tm_cur);
-    tma_prefetch_desc(&tm_prev);
-    tma_prefetch_desc(&tm_arr);
-    tma_prefetch_desc(&tm_upd);
+    {
+      const StepMaps m = maps_of(pr_it);
+      tma_prefetch_desc(m.cur);
+      tma_prefetch_desc(m.prev);
+      tma_prefetch_desc(m.arr);
+      tma_prefetch_desc(m.upd);
+    }
     // Prologue: the first S-2 steps of this CTA.
     for (int a = 0; a < S - 2 && pr_item < P.nitems; ++a) {
-      issue_step<TY>(smem + pr_stage * G::STAGE_B, &full[pr_stage], pr_it, pr_k, &tm_cur, &tm_prev, &tm_arr, &tm_upd);
+      issue_step<TY>(smem + pr_stage * G::STAGE_B, &full[pr_stage], pr_it, pr_k, maps_of(pr_it));
       if (++pr_stage == S) pr_stage = 0;
       if (++pr_k >= pr_it.z1 + kRadius) {
         pr_item += gridDim.x;
         if (pr_item < P.nitems) {
-          pr_it = decode_item<TY>(pr_item, P);
+          pr_it = decode_item<TY, BATCH>(pr_item, P);
           pr_k = pr_it.z0 - kRadius;
         }
       }
@@ -216,14 +252,17 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   uint32_t phase = 0, xphase = 0;
   int dsel = 0;
   for (int item = blockIdx.x; item < P.nitems; item += gridDim.x) {
-    const Item it = decode_item<TY>(item, P);
+    const Item it = decode_item<TY, BATCH>(item, P);
+    const ShotDesc &sd = BATCH ? P.shots[it.shot] : P.one;
     const int kbeg = it.z0 - kRadius;
     const int kend = it.z1 + kRadius;
     const int gx = it.x0 + lx;
     const int gy = it.y0 + ly;
-    const bool valid = (gx >= P.bord) && (gx < P.sx - P.bord) && (gy >= P.bord) && (gy < P.sy - P.bord);
-    unsigned long long *out = reinterpret_cast<unsigned long long *>(P.prev) + ((long)gy * P.pitch + gx);
-    const long plane = (long)P.pitch * P.sy;
+    const int bord = sd.bord, sxs = sd.sx, sys = sd.sy;
+    const bool valid = (gx >= bord) && (gx < sxs - bord) && (gy >= bord) && (gy < sys - bord);
+    const long plane = (long)sd.pitch * sys;
+    unsigned long long *out = reinterpret_cast<unsigned long long *>(sd.F[P.parity ^ 1]) + ((long)gy * sd.pitch + gx);
+    const int src_z = sd.src_z, cor_z = sd.cor_z;  // cells are read from `sd` on the (rare) planes
     const int ci = ly * G::TX + lx;
     const int hc = (ly + kRadius) * G::HX + (lx + kRadius);
 
@@ -242,7 +281,7 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
         }
         const bool center = (k >= it.z0) && (k < it.z1);
         const bool upd = (k - kRadius >= it.z0);
-        const bool src_plane = (k == P.src_z);
+        const bool src_plane = (k == src_z);
         const f2 *H = reinterpret_cast<const f2 *>(st);
 
         f2 c = H[hc];
@@ -258,11 +297,11 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
         // current p and q gain `src` at the source cell before the update
         // reads them; added to this thread's copies of the plane.
         if (src_plane) {
+          const int src_x = sd.src_x, src_y = sd.src_y;
           const f2 sv = splat(P.src);
           f2 dummy;
-          if (gy == P.src_y && abs(P.src_x - gx) <= kRadius) add_at(c, xa, xb, P.src_x - gx, sv);
-          if (gx == P.src_x && P.src_y != gy && abs(P.src_y - gy) <= kRadius)
-            add_at(dummy, ya, yb, P.src_y - gy, sv);
+          if (gy == src_y && abs(src_x - gx) <= kRadius) add_at(c, xa, xb, src_x - gx, sv);
+          if (gx == src_x && src_y != gy && abs(src_y - gy) <= kRadius) add_at(dummy, ya, yb, src_y - gy, sv);
         }
         const f2 d1x = scale<ISO>(d1(xa[0], xb[0], xa[1], xb[1], xa[2], xb[2], xa[3], xb[3]), sx1);
         const f2 d1y = scale<ISO>(d1(ya[0], yb[0], ya[1], yb[1], ya[2], yb[2], ya[3], yb[3]), sy1);
@@ -283,10 +322,11 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
               hb[o - 1] = H[hh - o * G::HX];
             }
             if (src_plane) {
+              const int src_x = sd.src_x, src_y = sd.src_y;
               const int hgy = it.y0 + hr;
-              if (hxc == P.src_x - (it.x0 - kRadius) && P.src_y != hgy && abs(P.src_y - hgy) <= kRadius) {
+              if (hxc == src_x - (it.x0 - kRadius) && src_y != hgy && abs(src_y - hgy) <= kRadius) {
                 f2 dummy;
-                add_at(dummy, ha, hb, P.src_y - hgy, splat(P.src));
+                add_at(dummy, ha, hb, src_y - hgy, splat(P.src));
               }
             }
             db[hr * G::HX + hxc] = scale<ISO>(d1(ha[0], hb[0], ha[1], hb[1], ha[2], hb[2], ha[3], hb[3]), sy1);
@@ -302,13 +342,12 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
         // the next step due (S-2 steps ahead of this one).
         if (producer && pr_item < P.nitems) {
           fence_proxy_async_smem();
-          issue_step<TY>(smem + pr_stage * G::STAGE_B, &full[pr_stage], pr_it, pr_k, &tm_cur, &tm_prev, &tm_arr,
-                         &tm_upd);
+          issue_step<TY>(smem + pr_stage * G::STAGE_B, &full[pr_stage], pr_it, pr_k, maps_of(pr_it));
           if (++pr_stage == S) pr_stage = 0;
           if (++pr_k >= pr_it.z1 + kRadius) {
             pr_item += gridDim.x;
             if (pr_item < P.nitems) {
-              pr_it = decode_item<TY>(pr_item, P);
+              pr_it = decode_item<TY, BATCH>(pr_item, P);
               pr_k = pr_it.z0 - kRadius;
             }
           }
@@ -337,8 +376,8 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
           const float rhsq = __fmaf_rn(-v2sz, __fsub_rn(h2p, h2q), __fmaf_rn(v2pn, h2p, t));
           f2 old = reinterpret_cast<const f2 *>(st + G::OFF_PP)[ci];
           const int zc = k - kRadius;
-          if (zc == P.cor_z) {
-            if (gx == P.cor_x && gy == P.cor_y) old = add2(old, splat(P.cor));
+          if (zc == cor_z) {
+            if (gx == sd.cor_x && gy == sd.cor_y) old = add2(old, splat(P.cor));
           }
           const f2 cur = Pr[cs];
           const f2 nw = fma2(mk2(rhsp, rhsq), splat(P.dt2), sub2(add2(cur, cur), old));
@@ -383,12 +422,13 @@ aborted:
 
 template <int TY, int S, int MINB>
 static cudaError_t launch_t(const PropLaunch &L, cudaStream_t s) {
-  const bool iso = L.p.iso != 0;
   constexpr size_t smem = smem_bytes<TY, S>();
-  auto kern = iso ? k_propagate_fp32<TY, S, true, MINB> : k_propagate_fp32<TY, S, false, MINB>;
+  const bool iso = L.p.iso != 0;
+  auto kern = L.batch ? (iso ? k_propagate_fp32<TY, S, true, true, MINB> : k_propagate_fp32<TY, S, false, true, MINB>)
+                      : (iso ? k_propagate_fp32<TY, S, true, false, MINB> : k_propagate_fp32<TY, S, false, false, MINB>);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  kern<<<L.grid, kTileX * TY, smem, s>>>(L.cur_halo, L.prev_pt, L.coef_arr, L.coef_upd, L.p);
+  kern<<<L.grid, kTileX * TY, smem, s>>>(L.m, L.p);
   return cudaGetLastError();
 }
 

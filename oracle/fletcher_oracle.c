@@ -406,3 +406,46 @@ void orc_quantize_planes(int sx, int sy, int sz, float *f) {
     for (long i = z * plane; i < (z + 1) * plane; i++) f[i] = q16(f[i], scale, inv);
   }
 }
+
+/* Other 16/24-bit storage candidates for the same experiment:
+ * mode 1: 16-bit fixed point per plane, value = k * 2^(e-15), |k| <= 32767,
+ *         with 2^e >= the plane's largest magnitude (block floating point);
+ * mode 2: FP16 plus an 8-bit mantissa extension: the float rounded to 19
+ *         significant bits (round to nearest even on the 5 dropped bits). */
+static float qfix16(float v, float scale, float inv) {
+  float k = rintf(v * scale);
+  if (k > 32767.0f) k = 32767.0f;
+  if (k < -32767.0f) k = -32767.0f;
+  return k * inv;
+}
+static float q19(float v) {
+  uint32_t u;
+  memcpy(&u, &v, 4);
+  const uint32_t lsb = (u >> 5) & 1u;
+  u = (u + 0xFu + lsb) & ~0x1Fu;
+  float r;
+  memcpy(&r, &u, 4);
+  return r;
+}
+void orc_quantize_planes_mode(int sx, int sy, int sz, float *f, int mode) {
+  if (mode == 0) {
+    orc_quantize_planes(sx, sy, sz, f);
+    return;
+  }
+  const long plane = (long)sx * sy;
+#pragma omp parallel for schedule(static)
+  for (int z = 0; z < sz; z++) {
+    if (mode == 2) {
+      for (long i = z * plane; i < (z + 1) * plane; i++) f[i] = q19(f[i]);
+      continue;
+    }
+    float m = 0.0f;
+    for (long i = z * plane; i < (z + 1) * plane; i++) m = fmaxf(m, fabsf(f[i]));
+    if (m == 0.0f) continue;
+    int e;
+    frexpf(m, &e);
+    if (e < -100) e = -100;
+    const float scale = ldexpf(1.0f, 15 - e), inv = ldexpf(1.0f, e - 15);
+    for (long i = z * plane; i < (z + 1) * plane; i++) f[i] = qfix16(f[i], scale, inv);
+  }
+}
