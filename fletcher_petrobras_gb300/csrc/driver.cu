@@ -627,3 +627,342 @@ extern "C" double FLETCHER_BytesPerCell(void) {
   // current (p,q) 8 B + previous (p,q) 8 B + ten coefficients 40 B + next (p,q) 8 B.
   return 64.0;
 }
+
+// ===== Batched shots ==============================================================
+//
+// Many independent shots of different sizes advance together: one persistent
+// launch per time step covers the work items of every shot that is still
+// running, and the whole time loop is captured in a CUDA graph.  Shots are
+// ordered by step count (longest first), so the shots still running at any
+// step are a prefix of that order and so are their work items.
+
+#include <algorithm>
+#include <vector>
+
+namespace {
+
+struct BatchShot {
+  int sx = 0, sy = 0, sz = 0, pitch = 0, nsteps = 0;
+  long isrc = 0;
+  size_t n = 0, npitch = 0;
+  float2 *F[2] = {nullptr, nullptr};
+  float *coef = nullptr;
+  int ntx = 0, nty = 0, chunk = 0, nchunk = 0;
+};
+
+struct Batch {
+  bool open = false;
+  int bord = 4;
+  float dx = 0, dy = 0, dz = 0, dt = 0;
+  std::vector<BatchShot> shots;
+  std::vector<int> order;      // shot indices, longest run first
+  std::vector<int> items_upto; // items of order[0..i]
+  int sealed_rows = 0;
+  ShotDesc *d_desc = nullptr;
+  ShotMaps *d_maps = nullptr;
+  int4 *d_items = nullptr;
+  float *scratch = nullptr;
+  size_t max_n = 0;
+  int rows = 12, stages = 5;
+  long launches = 0;
+  size_t dev_bytes = 0;
+  int num_sms = 0;
+  unsigned *err_host = nullptr, *err_dev = nullptr;
+  std::vector<float> src;      // source values of the last run
+};
+Batch B;
+
+void batch_free_tables() {
+  if (B.d_desc) cudaFree(B.d_desc);
+  if (B.d_maps) cudaFree(B.d_maps);
+  if (B.d_items) cudaFree(B.d_items);
+  B.d_desc = nullptr;
+  B.d_maps = nullptr;
+  B.d_items = nullptr;
+  B.sealed_rows = 0;
+}
+
+void batch_free() {
+  batch_free_tables();
+  for (auto &s : B.shots) {
+    if (s.F[0]) cudaFree(s.F[0]);
+    if (s.F[1]) cudaFree(s.F[1]);
+    if (s.coef) cudaFree(s.coef);
+  }
+  if (B.scratch) cudaFree(B.scratch);
+  if (B.err_host) cudaFreeHost(B.err_host);
+  B = Batch();
+}
+
+// Work list, descriptors and TMA descriptors for tile height `rows`.
+int batch_seal(int rows, int stages) {
+  if (!propagate_fp32_supported(rows, stages))
+    return fail(FLETCHER_ERR_ARGS, "tile shape (%d rows, %d stages) is not built", rows, stages);
+  if (B.sealed_rows == rows) {
+    B.stages = stages;
+    return FLETCHER_OK;
+  }
+  batch_free_tables();
+  const int ns = (int)B.shots.size();
+  std::vector<ShotDesc> desc(ns);
+  std::vector<ShotMaps> maps(ns);
+  std::vector<int4> items;
+  B.order.resize(ns);
+  for (int i = 0; i < ns; ++i) B.order[i] = i;
+  std::stable_sort(B.order.begin(), B.order.end(),
+                   [](int a, int b) { return B.shots[a].nsteps > B.shots[b].nsteps; });
+  B.items_upto.assign(ns, 0);
+  for (int oi = 0; oi < ns; ++oi) {
+    const int i = B.order[oi];
+    BatchShot &s = B.shots[i];
+    const int depth = s.sz - 2 * B.bord;
+    s.ntx = (s.sx - B.bord - kRadius + kTileX - 1) / kTileX;
+    s.nty = (s.sy - B.bord - kRadius + rows - 1) / rows;
+    s.nchunk = (depth + 127) / 128;
+    s.chunk = (depth + s.nchunk - 1) / s.nchunk;
+    s.nchunk = (depth + s.chunk - 1) / s.chunk;
+    if (build_maps(&maps[i], s.F, s.coef, s.sx, s.sy, s.sz, s.pitch, rows)) return g_last_err;
+    ShotDesc &d = desc[i];
+    memset(&d, 0, sizeof(d));
+    d.F[0] = s.F[0];
+    d.F[1] = s.F[1];
+    d.sx = s.sx; d.sy = s.sy; d.sz = s.sz; d.pitch = s.pitch; d.bord = B.bord;
+    d.ntx = s.ntx; d.nty = s.nty; d.chunk = s.chunk;
+    d.src_x = (int)(s.isrc % s.sx);
+    d.src_y = (int)((s.isrc / s.sx) % s.sy);
+    d.src_z = (int)(s.isrc / ((long)s.sx * s.sy));
+    d.cor_x = d.src_x; d.cor_y = d.src_y; d.cor_z = d.src_z;
+    const size_t base = items.size();
+    items.resize(base + (size_t)s.ntx * s.nty * s.nchunk);
+    fill_items(items.data() + base, i, s.ntx, s.nty, s.nchunk, rows);
+    B.items_upto[oi] = (int)items.size();
+  }
+  CK(cudaMalloc(&B.d_desc, sizeof(ShotDesc) * ns));
+  CK(cudaMalloc(&B.d_maps, sizeof(ShotMaps) * ns));
+  CK(cudaMalloc(&B.d_items, sizeof(int4) * items.size()));
+  CK(cudaMemcpy(B.d_desc, desc.data(), sizeof(ShotDesc) * ns, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(B.d_maps, maps.data(), sizeof(ShotMaps) * ns, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(B.d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
+  B.sealed_rows = rows;
+  B.stages = stages;
+  return FLETCHER_OK;
+}
+
+int batch_max_steps() {
+  int m = 0;
+  for (auto &s : B.shots) m = std::max(m, s.nsteps);
+  return m;
+}
+
+// Issues steps [it0, it1) of the time loop on the stream (no synchronisation).
+int batch_issue(int it0, int it1, const float *src) {
+  const int ns = (int)B.shots.size();
+  PropLaunch L;
+  memset(&L, 0, sizeof(L));
+  L.batch = true;
+  L.tile_rows = B.sealed_rows;
+  L.stages = B.stages;
+  PropParams &P = L.p;
+  P.shots = B.d_desc;
+  P.maps = B.d_maps;
+  P.items = B.d_items;
+  P.inv_dx = 1.0f / B.dx;
+  P.inv_dy = 1.0f / B.dy;
+  P.inv_dz = 1.0f / B.dz;
+  P.inv_dxx = 1.0f / (B.dx * B.dx);
+  P.inv_dyy = 1.0f / (B.dy * B.dy);
+  P.inv_dzz = 1.0f / (B.dz * B.dz);
+  P.iso = (B.dx == B.dy && B.dx == B.dz) ? 1 : 0;
+  P.dt2 = P.iso ? (B.dt * B.dt) * P.inv_dxx : B.dt * B.dt;
+  P.err = B.err_dev;
+  const int ctas = B.num_sms * propagate_fp32_ctas_per_sm(B.sealed_rows);
+  int active = ns;  // shots still running, a prefix of B.order
+  for (int it = it0; it < it1; ++it) {
+    while (active > 0 && B.shots[B.order[active - 1]].nsteps <= it) --active;
+    if (active == 0) break;
+    P.nitems = B.items_upto[active - 1];
+    P.parity = it & 1;
+    P.src = src[it];
+    P.cor = it > 0 ? src[it - 1] : 0.0f;
+    L.grid = P.nitems < ctas ? P.nitems : ctas;
+    CK(propagate_fp32_launch(L, g_stream));
+    ++B.launches;
+  }
+  return FLETCHER_OK;
+}
+
+}  // namespace
+
+extern "C" int FLETCHER_BatchCreate(int bord, float dx, float dy, float dz, float dt) {
+  batch_free();
+  if (bord < kRadius) return fail(FLETCHER_ERR_ARGS, "bord (%d) must be at least %d", bord, kRadius);
+  if (!(dx > 0.f) || !(dy > 0.f) || !(dz > 0.f)) return fail(FLETCHER_ERR_ARGS, "grid spacing must be positive");
+  if (ensure_stream()) return g_last_err;
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&B.num_sms, cudaDevAttrMultiProcessorCount, dev));
+  CK(cudaHostAlloc(&B.err_host, sizeof(unsigned), cudaHostAllocMapped));
+  *B.err_host = 0;
+  CK(cudaHostGetDevicePointer((void **)&B.err_dev, B.err_host, 0));
+  B.open = true;
+  B.bord = bord;
+  B.dx = dx; B.dy = dy; B.dz = dz; B.dt = dt;
+  B.rows = g_req_rows ? g_req_rows : 12;
+  B.stages = g_req_stages ? g_req_stages : 5;
+  return FLETCHER_OK;
+}
+
+extern "C" int FLETCHER_BatchAddShot(int sx, int sy, int sz, const float *model, long iSource, int nsteps) {
+  if (!B.open) return -fail(FLETCHER_ERR_ARGS, "FLETCHER_BatchAddShot before FLETCHER_BatchCreate");
+  const int b = B.bord;
+  if (sx <= 2 * b || sy <= 2 * b || sz <= 2 * b || !model || nsteps < 0)
+    return -fail(FLETCHER_ERR_ARGS, "bad shot %dx%dx%d", sx, sy, sz);
+  BatchShot s;
+  s.sx = sx; s.sy = sy; s.sz = sz; s.nsteps = nsteps; s.isrc = iSource;
+  s.pitch = (sx + 31) / 32 * 32;
+  s.n = (size_t)sx * sy * sz;
+  s.npitch = (size_t)s.pitch * sy * sz;
+  const long x = iSource % sx, y = (iSource / sx) % sy, z = iSource / ((long)sx * sy);
+  if (iSource < 0 || (size_t)iSource >= s.n || x < b || x >= sx - b || y < b || y >= sy - b || z < b ||
+      z >= sz - b)
+    return -fail(FLETCHER_ERR_ARGS, "batched source %ld must lie in the updated region", iSource);
+  cudaStream_t st = g_stream;
+  if (cudaMalloc(&s.F[0], s.npitch * sizeof(float2)) != cudaSuccess ||
+      cudaMalloc(&s.F[1], s.npitch * sizeof(float2)) != cudaSuccess ||
+      cudaMalloc(&s.coef, s.npitch * kNumCoef * sizeof(float)) != cudaSuccess) {
+    if (s.F[0]) cudaFree(s.F[0]);
+    if (s.F[1]) cudaFree(s.F[1]);
+    if (s.coef) cudaFree(s.coef);
+    cudaGetLastError();
+    return -fail(FLETCHER_ERR_NOMEM, "device allocation for shot %zu failed", B.shots.size());
+  }
+  float *raw = nullptr;
+  if (cudaMalloc(&raw, 6 * s.n * sizeof(float)) != cudaSuccess) {
+    cudaFree(s.F[0]); cudaFree(s.F[1]); cudaFree(s.coef);
+    cudaGetLastError();
+    return -fail(FLETCHER_ERR_NOMEM, "device allocation for shot %zu failed", B.shots.size());
+  }
+  cudaError_t e = cudaMemcpyAsync(raw, model, 6 * s.n * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s.coef, 0, s.npitch * kNumCoef * sizeof(float), st);
+  if (e == cudaSuccess) {
+    k_precompute<<<grid_for(s.n), 256, 0, st>>>(raw, s.coef, sx, sy, sz, s.pitch);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemsetAsync(s.F[0], 0, s.npitch * sizeof(float2), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s.F[1], 0, s.npitch * sizeof(float2), st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(raw);
+  if (e != cudaSuccess) return -fail(FLETCHER_ERR_CUDA, "shot set-up: %s", cudaGetErrorString(e));
+  B.dev_bytes += 2 * s.npitch * sizeof(float2) + s.npitch * kNumCoef * sizeof(float);
+  if (s.n > B.max_n) {
+    if (B.scratch) cudaFree(B.scratch);
+    B.scratch = nullptr;
+    if (cudaMalloc(&B.scratch, s.n * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      return -fail(FLETCHER_ERR_NOMEM, "read-back buffer allocation failed");
+    }
+    B.max_n = s.n;
+  }
+  B.shots.push_back(s);
+  batch_free_tables();
+  return (int)B.shots.size() - 1;
+}
+
+extern "C" int FLETCHER_BatchReset(void) {
+  if (!B.open) return fail(FLETCHER_ERR_ARGS, "no batch");
+  for (auto &s : B.shots) {
+    CK(cudaMemsetAsync(s.F[0], 0, s.npitch * sizeof(float2), g_stream));
+    CK(cudaMemsetAsync(s.F[1], 0, s.npitch * sizeof(float2), g_stream));
+  }
+  CK(cudaStreamSynchronize(g_stream));
+  return FLETCHER_OK;
+}
+
+extern "C" int FLETCHER_BatchRun(const float *src, int use_graph, float *elapsed_ms) {
+  if (!B.open || B.shots.empty()) return fail(FLETCHER_ERR_ARGS, "empty batch");
+  if (!src) return fail(FLETCHER_ERR_ARGS, "source values missing");
+  if (batch_seal(B.rows, B.stages)) return g_last_err;
+  const int steps = batch_max_steps();
+  B.src.assign(src, src + steps);
+  // Kernel attributes are set outside any capture.
+  if (propagate_fp32_prepare(B.sealed_rows, B.stages) != cudaSuccess)
+    return fail(FLETCHER_ERR_CUDA, "kernel attribute set-up failed");
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  cudaGraphExec_t exec = nullptr;
+  if (use_graph) {
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(g_stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = batch_issue(0, steps, src);
+    cudaError_t ce = cudaStreamEndCapture(g_stream, &graph);
+    if (rc) return rc;
+    CK(ce);
+    CK(cudaGraphInstantiate(&exec, graph, 0));
+    CK(cudaGraphDestroy(graph));
+    CK(cudaGraphUpload(exec, g_stream));
+  }
+  CK(cudaEventRecord(e0, g_stream));
+  if (use_graph) {
+    CK(cudaGraphLaunch(exec, g_stream));
+  } else if (batch_issue(0, steps, src)) {
+    return g_last_err;
+  }
+  CK(cudaEventRecord(e1, g_stream));
+  CK(cudaStreamSynchronize(g_stream));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  if (elapsed_ms) *elapsed_ms = ms;
+  if (exec) cudaGraphExecDestroy(exec);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (*(volatile unsigned *)B.err_host)
+    return fail(FLETCHER_ERR_TIMEOUT, "a batched propagate kernel gave up waiting (error word 0x%x)",
+                *(volatile unsigned *)B.err_host);
+  return FLETCHER_OK;
+}
+
+extern "C" int FLETCHER_BatchGetField(int shot, int which, float *host) {
+  if (!B.open || shot < 0 || shot >= (int)B.shots.size() || which < 0 || which > 3 || !host)
+    return fail(FLETCHER_ERR_ARGS, "bad shot %d or field %d", shot, which);
+  const BatchShot &s = B.shots[shot];
+  // After nsteps steps the current field is in F[nsteps & 1].
+  const int buf = which < 2 ? (s.nsteps & 1) : ((s.nsteps + 1) & 1);
+  k_unpack<<<grid_for(s.n), 256, 0, g_stream>>>(s.F[buf], B.scratch, which & 1, s.sx, s.sy, s.sz, s.pitch);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(host, B.scratch, s.n * sizeof(float), cudaMemcpyDeviceToHost, g_stream));
+  CK(cudaStreamSynchronize(g_stream));
+  // The previous-field buffer lacks the last step's source at the source
+  // cell (the next step would add it when reading): add it here, as the
+  // reference's in-place InsertSource leaves it.
+  if (which >= 2 && s.nsteps > 0 && (size_t)s.nsteps <= B.src.size())
+    host[s.isrc] = host[s.isrc] + B.src[s.nsteps - 1];
+  return FLETCHER_OK;
+}
+
+extern "C" int FLETCHER_BatchSetTileConfig(int rows, int stages) {
+  if (!B.open) return fail(FLETCHER_ERR_ARGS, "no batch");
+  const int r = rows ? rows : 12, s = stages ? stages : 5;
+  if (!propagate_fp32_supported(r, s)) return fail(FLETCHER_ERR_ARGS, "tile shape (%d, %d) is not built", r, s);
+  B.rows = r;
+  B.stages = s;
+  return FLETCHER_OK;
+}
+
+extern "C" int FLETCHER_BatchInfo(long *nshots, double *cell_steps, long *launches, size_t *device_bytes) {
+  if (nshots) *nshots = (long)B.shots.size();
+  if (cell_steps) {
+    double c = 0.0;
+    for (auto &s : B.shots)
+      c += (double)(s.sx - 2 * B.bord) * (s.sy - 2 * B.bord) * (s.sz - 2 * B.bord) * s.nsteps;
+    *cell_steps = c;
+  }
+  if (launches) *launches = B.launches;
+  if (device_bytes) *device_bytes = B.dev_bytes;
+  return FLETCHER_OK;
+}
+
+extern "C" void FLETCHER_BatchDestroy(void) {
+  if (g_stream) cudaStreamSynchronize(g_stream);
+  batch_free();
+}

@@ -76,6 +76,7 @@ size_t propagate_fp32_smem_bytes(int tile_rows, int stages);
 bool propagate_fp32_supported(int tile_rows, int stages);
 int propagate_fp32_threads(int tile_rows);
 int propagate_fp32_ctas_per_sm(int tile_rows);
+cudaError_t propagate_fp32_prepare(int tile_rows, int stages);
 cudaError_t propagate_fp32_launch(const PropLaunch &L, cudaStream_t s);
 
 // Time limit of every device-side wait (ns).

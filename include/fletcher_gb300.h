@@ -118,6 +118,38 @@ size_t FLETCHER_DeviceBytes(void);
  * next field). */
 double FLETCHER_BytesPerCell(void);
 
+/* ---- Batched shots (no counterpart in the reference, whose runs are one
+ * shot per process).  Independent shots of different sizes share one
+ * persistent launch per time step; the time loop runs as one CUDA graph.
+ * All shots share bord, spacing and time step; each has its own grid,
+ * model, source cell (inside the updated region) and step count.  The
+ * single-shot state of part 1 is separate and unaffected. */
+
+/* Starts an empty batch (frees a previous one). */
+int FLETCHER_BatchCreate(int bord, float dx, float dy, float dz, float dt);
+/* Adds a shot: grid sx*sy*sz, model = vpz vsv epsilon delta phi theta
+ * (sx*sy*sz floats each, consecutive, boundary already applied), source
+ * index, number of steps.  Copies the model to the GPU and computes its
+ * coefficients in FP64.  Returns the shot index (>= 0) or -status. */
+int FLETCHER_BatchAddShot(int sx, int sy, int sz, const float *model, long iSource, int nsteps);
+/* Tile shape for the next FLETCHER_BatchRun (0 = default). */
+int FLETCHER_BatchSetTileConfig(int tile_rows, int stages);
+/* Runs every shot from its current state for its own step count: step it
+ * adds src[it] at each running shot's source cell (the reference's
+ * InsertSource) then advances.  use_graph != 0 captures the loop in a CUDA
+ * graph first.  *elapsed_ms (may be NULL) = device time of the loop. */
+int FLETCHER_BatchRun(const float *src, int use_graph, float *elapsed_ms);
+/* Zeroes every shot's fields (the coefficients stay). */
+int FLETCHER_BatchReset(void);
+/* Copies one field of a shot after the run: which = 0 current p, 1 current
+ * q, 2 previous p, 3 previous q (as the reference leaves them: the previous
+ * fields include the last step's source). */
+int FLETCHER_BatchGetField(int shot, int which, float *host);
+/* Shots, sum over shots of updated cells x steps, kernel launches issued,
+ * device bytes held. */
+int FLETCHER_BatchInfo(long *nshots, double *cell_steps, long *launches, size_t *device_bytes);
+void FLETCHER_BatchDestroy(void);
+
 /* No counterpart in the reference.  Read-back for callers that cannot
  * allocate device memory: codes that reserve the whole GPU for their own
  * wavefield and coefficient volumes up front, or whose time loop must not

@@ -133,3 +133,16 @@ def test_reference_front_end_links_against_library(tmp_path):
     subprocess.run(["gcc", "-o", str(exe), *objs, "-L" + OUT, "-lfletcher_gb300", "-Wl,-rpath," + OUT, "-lm"],
                    check=True)
     assert exe.exists()
+
+
+def test_multishot_spec_properties():
+    from fletcher_petrobras_gb300.batch import multishot_spec
+
+    spec = multishot_spec(48, seed=0)
+    assert len(spec) == 48
+    for p in spec:
+        assert all(96 <= v <= 320 and v % 8 == 0 for v in (p.nx, p.ny, p.nz))
+        assert 500 <= p.steps <= 1500 and p.dt == pytest.approx(0.0006)
+        ix, iy, iz = p.src_xyz
+        b = p.bord + p.absorb
+        assert b <= iz < b + max(1, p.nz // 4) and b <= ix < b + p.nx and b <= iy < b + p.ny
