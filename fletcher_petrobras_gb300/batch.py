@@ -59,13 +59,14 @@ class Batch:
         if self.lib.FLETCHER_BatchSetTileConfig(rows, stages):
             _check(self.lib, "FLETCHER_BatchSetTileConfig")
 
-    def run(self, use_graph: bool = True, fcut: float | None = None) -> float:
-        """Runs every shot for its own step count; returns the device time in ms."""
+    def run(self, use_graph: bool = True, fcut: float | None = None, max_steps: int = 0) -> float:
+        """Runs every shot for its own step count (or the first max_steps steps);
+        returns the device time in ms."""
         steps = max(p.steps for p in self.probs)
         fc = self.probs[0].fcut if fcut is None else fcut
         src = np.array([self.lib.FLETCHER_Source(self.dt, it, fc) for it in range(steps)], np.float32)
         ms = C.c_float(0.0)
-        if self.lib.FLETCHER_BatchRun(fptr(src), 1 if use_graph else 0, C.byref(ms)):
+        if self.lib.FLETCHER_BatchRun(fptr(src), int(max_steps), 1 if use_graph else 0, C.byref(ms)):
             _check(self.lib, "FLETCHER_BatchRun")
         return float(ms.value)
 
@@ -87,3 +88,10 @@ class Batch:
 
     def close(self):
         self.lib.FLETCHER_BatchDestroy()
+
+
+def shape_class(probs) -> str:
+    """Cache key part: shot count and the rounded median interior size."""
+    ns = sorted(p.nx * p.ny * p.nz for p in probs)
+    med = int(round(ns[len(ns) // 2] ** (1 / 3) / 32.0)) * 32
+    return f"batch{len(probs)}-n{med}"

@@ -54,7 +54,7 @@ struct Geo {
 
 template <int TY, int S>
 constexpr size_t smem_bytes() {
-  return size_t(S) * Geo<TY>::STAGE_B + Geo<TY>::DBUF_B + 8 * S + 8 + 16 + 128;
+  return size_t(S) * Geo<TY>::STAGE_B + Geo<TY>::DBUF_B + 8 * S + 8 + 16 + 64 + 128;  // + producer cursor
 }
 
 // A work item resolved against its shot: tile origin, z range, and (batched
@@ -93,6 +93,13 @@ __device__ __forceinline__ Item decode_item(int item, const PropParams &P) {
 // Descriptors used for one step of item `it`.
 struct StepMaps {
   const CUtensorMap *cur, *prev, *arr, *upd;
+};
+
+// The producer's position (next step to load), kept in shared memory so it
+// costs no registers in the other threads.
+struct Cursor {
+  Item it;
+  int item, k, stage;
 };
 
 // Issues the TMA loads of one step (plane k of item `it`) into `stage`.
@@ -189,7 +196,7 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
 
   if (blockIdx.x >= P.nitems) return;
   // The producer is lane 0 of the last warp (warps 0 .. TY/4-1 carry the
-  // halo-column work).  Its cursor (pr_*) is the next step to load.
+  // halo-column work).  Its cursor, in shared memory, is the next step to load.
   const bool producer = tid == (TY - 1) * 32;
   auto maps_of = [&](const Item &it) {
     StepMaps m;
@@ -207,35 +214,46 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
     }
     return m;
   };
-  Item pr_it = decode_item<TY, BATCH>(blockIdx.x, P);
-  int pr_item = blockIdx.x, pr_k = pr_it.z0 - kRadius, pr_stage = 0;
+  Cursor *cur = reinterpret_cast<Cursor *>(s_abort + 4);
+  // Issues the cursor's step into its stage and advances the cursor.
+  auto produce = [&]() {
+    Cursor c = *cur;
+    issue_step<TY>(smem + c.stage * G::STAGE_B, &full[c.stage], c.it, c.k, maps_of(c.it));
+    if (++c.stage == S) c.stage = 0;
+    if (++c.k >= c.it.z1 + kRadius) {
+      c.item += gridDim.x;
+      if (c.item < P.nitems) {
+        c.it = decode_item<TY, BATCH>(c.item, P);
+        c.k = c.it.z0 - kRadius;
+      }
+    }
+    *cur = c;
+  };
   if (tid == 0) {
     for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
     mbar_init(xchg, TY);
     mbar_fence_init();
     *s_abort = 0;
   }
+  if (producer) {
+    Cursor c;
+    c.it = decode_item<TY, BATCH>(blockIdx.x, P);
+    c.item = blockIdx.x;
+    c.k = c.it.z0 - kRadius;
+    c.stage = 0;
+    *cur = c;
+  }
   __syncthreads();
   if (producer) {
     {
-      const StepMaps m = maps_of(pr_it);
+      const StepMaps m = maps_of(cur->it);
       tma_prefetch_desc(m.cur);
       tma_prefetch_desc(m.prev);
       tma_prefetch_desc(m.arr);
       tma_prefetch_desc(m.upd);
     }
     // Prologue: the first S-2 steps of this CTA.
-    for (int a = 0; a < S - 2 && pr_item < P.nitems; ++a) {
-      issue_step<TY>(smem + pr_stage * G::STAGE_B, &full[pr_stage], pr_it, pr_k, maps_of(pr_it));
-      if (++pr_stage == S) pr_stage = 0;
-      if (++pr_k >= pr_it.z1 + kRadius) {
-        pr_item += gridDim.x;
-        if (pr_item < P.nitems) {
-          pr_it = decode_item<TY, BATCH>(pr_item, P);
-          pr_k = pr_it.z0 - kRadius;
-        }
-      }
-    }
+    for (int a = 0; a < S - 2 && cur->item < P.nitems; ++a) produce();
   }
 
   // Spacing factors (unused on isotropic grids).
@@ -340,17 +358,9 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
         // The producer has passed the exchange of the previous step, so every
         // thread is past the step before it: refill that step's stage with
         // the next step due (S-2 steps ahead of this one).
-        if (producer && pr_item < P.nitems) {
+        if (producer && cur->item < P.nitems) {
           fence_proxy_async_smem();
-          issue_step<TY>(smem + pr_stage * G::STAGE_B, &full[pr_stage], pr_it, pr_k, maps_of(pr_it));
-          if (++pr_stage == S) pr_stage = 0;
-          if (++pr_k >= pr_it.z1 + kRadius) {
-            pr_item += gridDim.x;
-            if (pr_item < P.nitems) {
-              pr_it = decode_item<TY, BATCH>(pr_item, P);
-              pr_k = pr_it.z0 - kRadius;
-            }
-          }
+          produce();
         }
         if (upd) {
           const int cs = (j + 5) % 9;  // ring slot of plane k-4

@@ -134,11 +134,13 @@ int FLETCHER_BatchCreate(int bord, float dx, float dy, float dz, float dt);
 int FLETCHER_BatchAddShot(int sx, int sy, int sz, const float *model, long iSource, int nsteps);
 /* Tile shape for the next FLETCHER_BatchRun (0 = default). */
 int FLETCHER_BatchSetTileConfig(int tile_rows, int stages);
-/* Runs every shot from its current state for its own step count: step it
- * adds src[it] at each running shot's source cell (the reference's
- * InsertSource) then advances.  use_graph != 0 captures the loop in a CUDA
- * graph first.  *elapsed_ms (may be NULL) = device time of the loop. */
-int FLETCHER_BatchRun(const float *src, int use_graph, float *elapsed_ms);
+/* Runs every shot from its current state for its own step count (or only
+ * the first max_steps steps when max_steps > 0, e.g. for tuning; read-back
+ * assumes a full run): step it adds src[it] at each running shot's source
+ * cell (the reference's InsertSource) then advances.  use_graph != 0
+ * captures the loop in a CUDA graph first.  *elapsed_ms (may be NULL) =
+ * device time of the loop. */
+int FLETCHER_BatchRun(const float *src, int max_steps, int use_graph, float *elapsed_ms);
 /* Zeroes every shot's fields (the coefficients stay). */
 int FLETCHER_BatchReset(void);
 /* Copies one field of a shot after the run: which = 0 current p, 1 current

@@ -236,6 +236,7 @@ def test_c1_full_size_vs_reference():
     assert prob == C1.with_(name=prob.name)
     p, q, _, _ = gpu_run(prob, prob.model(), use_run=True)
     s = meta["stride"]
-    assert rel_l2(subsample(p, prob, s), g["p"]) < TOL_C1
-    assert rel_l2(subsample(q, prob, s), g["q"]) < TOL_C1
-    assert rel_l2(np.sqrt(plane_sums(p, prob)), np.sqrt(g["psum"])) < TOL_C1
+    ep, eq = rel_l2(subsample(p, prob, s), g["p"]), rel_l2(subsample(q, prob, s), g["q"])
+    es = rel_l2(np.sqrt(plane_sums(p, prob)), np.sqrt(g["psum"]))
+    print(f"C1 504^3 x 1000 steps vs reference: rel L2 p {ep:.3e} q {eq:.3e} plane energy {es:.3e}")
+    assert ep < TOL_C1 and eq < TOL_C1 and es < TOL_C1
