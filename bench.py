@@ -171,6 +171,47 @@ def workload(args):
     return C1.with_(name=f"C1-layered-{n}", nx=n, ny=n, nz=n, source=(s // 2, s // 2, C1.bord + C1.absorb + 8))
 
 
+# Kernels one step launches in each storage form (the 16-bit forms set the
+# new planes' scales in a small kernel before the propagate kernel).
+LAUNCHES_PER_STEP = {"fp32": 1, "fp16": 2, "fp16x": 2}
+KERNEL = {"fp32": "k_propagate_fp32", "fp16": "k_propagate_half<EXT=false>", "fp16x": "k_propagate_half<EXT=true>"}
+
+
+def timed_run(prob, model, form, K, W, group, clocks=None):
+    """W untimed steps, then K steps timed with CUDA events on the library's
+    stream.  Returns (ms, kernel launches, bytes per cell, device GB)."""
+    import torch
+
+    from fletcher_petrobras_gb300 import Propagator
+
+    src = prob.sources(W + K)
+    stream = torch.cuda.Stream()
+    prop = Propagator(stream=stream.cuda_stream, form=form)
+    prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model)
+    prop.run(W, prob.i_source, src[:W])
+    prop.synchronize()
+    launches0 = prop.kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if clocks:
+        clocks.start()
+    group.barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    prop.run(K, prob.i_source, src[W:W + K])
+    ev1.record(stream)
+    prop.synchronize()
+    torch.cuda.synchronize()
+    group.barrier()
+    clk = clocks.stop() if clocks else None
+    ms = ev0.elapsed_time(ev1)
+    launches = (prop.kernel_launches() - launches0) * LAUNCHES_PER_STEP[form]
+    bpc = prop.bytes_per_cell()
+    dev_gb = prop.device_bytes() / 1e9
+    prop.finalize()
+    Propagator(form="fp32")
+    return ms, launches, bpc, dev_gb, clk
+
+
 def run_gb300(args, ws, rank, local, group):
     import torch
 
@@ -182,30 +223,8 @@ def run_gb300(args, ws, rank, local, group):
     prob = workload(args)
     K, W = args.steps, args.warmup
     model = prob.model()
-    src = prob.sources(W + K)
-    stream = torch.cuda.Stream()
-    prop = Propagator(stream=stream.cuda_stream)
-    prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model)
-    prop.run(W, prob.i_source, src[:W])
-    prop.synchronize()
-    launches0 = prop.kernel_launches()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clocks = ClockSampler(local)
-    clocks.start()
-    group.barrier()
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    prop.run(K, prob.i_source, src[W:W + K])
-    ev1.record(stream)
-    prop.synchronize()
-    torch.cuda.synchronize()
-    group.barrier()
-    clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    launches = prop.kernel_launches() - launches0
-    bpc = prop.bytes_per_cell()
-    dev_gb = prop.device_bytes() / 1e9
-    prop.finalize()
+    form = args.form
+    ms, launches, bpc, dev_gb, clk = timed_run(prob, model, form, K, W, group, ClockSampler(local))
 
     ms_max = group.reduce(ms, "max")
     cells = prob.updated_cells
@@ -213,7 +232,22 @@ def run_gb300(args, ws, rank, local, group):
     per_launch_s = ms / 1e3 / K
     achieved = bpc * cells / per_launch_s / 1e9
     peak, peak_kind = measured_peak()
-    tpc = ncu_traffic_per_cell()
+    tpc = ncu_traffic_per_cell() if form == "fp32" else None
+
+    # The other storage forms on the same workload (fewer steps).
+    forms = {}
+    if not args.no_forms:
+        for f in ("fp32", "fp16x", "fp16"):
+            if f == form:
+                continue
+            fk = max(1, min(K, args.form_steps))
+            fms, _, fbpc, _, _ = timed_run(prob, model, f, fk, W, group)
+            fms = group.reduce(fms, "max")
+            forms[f] = {"value": round(ws * cells * fk / (fms / 1e3) / 1e6, 1), "ms_per_step": round(fms / fk, 4),
+                        "steps": fk, "bytes_per_cell": fbpc,
+                        "hbm_gbs": round(fbpc * cells / (fms / 1e3 / fk) / 1e9, 1)}
+        for f in forms:
+            forms[f]["speedup_vs_this_form"] = round((ms_max / K) / forms[f]["ms_per_step"], 3)
 
     # End to end through the C ABI with host buffers (the reference's Model() sequence).
     import ctypes as C
@@ -222,12 +256,16 @@ def run_gb300(args, ws, rank, local, group):
     e2e = e2e_wall = None
     if not args.no_e2e:
         f = np.zeros((4, prob.n), np.float32)
+        from fletcher_petrobras_gb300.driver import FORMS
+
+        lib.FLETCHER_SetForm(FORMS[form])
         group.barrier()
         rc = lib.FLETCHER_Model(K, prob.i_source, prob.fcut, 0.01, prob.sx, prob.sy, prob.sz, prob.bord, prob.dx,
                                 prob.dy, prob.dz, prob.dt, *[fptr(f[k]) for k in range(4)],
                                 *[fptr(model[k]) for k in range(6)], stats)
         if rc:
             raise RuntimeError("FLETCHER_Model failed: " + lib.FLETCHER_GetLastErrorString().decode())
+        lib.FLETCHER_SetForm(FORMS["fp32"])
         e2e_wall = group.reduce(stats[2], "max")
         e2e = ws * cells * K / e2e_wall / 1e6
         del f
@@ -247,11 +285,11 @@ def run_gb300(args, ws, rank, local, group):
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
         "ms_per_step": round(ms_max / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded 8-layer TTI model, random-velocity boundary)",
-        "config": {"workload": f"C1: plain FP32 single shot, {prob.nx}^3 interior ({prob.sx}^3 grid), bord 4, "
+        "dtype": "f32" if form == "fp32" else "f32 arithmetic, " + form + " storage", "data": "synthetic (seeded 8-layer TTI model, random-velocity boundary)",
+        "config": {"workload": f"C1: {form.upper()} single shot, {prob.nx}^3 interior ({prob.sx}^3 grid), bord 4, "
                                f"absorb 32, dx 12.5 m, dt 0.6 ms, 8-layer seeded TTI, 15 Hz Ricker at {prob.src_xyz}",
                    "grid": [prob.sx, prob.sy, prob.sz], "updated_cells_per_step": cells,
-                   "form": "fp32", "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "form": form, "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": f"inputs resident in HBM ({dev_gb:.1f} GB) are larger than L2 (129 MB); no flush",
                    "timed_steps_include": "fused source injection + one propagate launch per step"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -259,7 +297,7 @@ def run_gb300(args, ws, rank, local, group):
                      "algorithmic_bytes_per_cell": bpc,
                      "traffic": None if tpc is None else round(tpc * cells / 1e9, 3),
                      "traffic_unit": "GB per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
-                     "kernel": "k_propagate_fp32"},
+                     "kernel": KERNEL[form]},
         "e2e": None if e2e is None else {
                 "value": round(e2e, 1), "unit": UNIT, "h2d_bytes_per_step": int(stats[3] / K),
                 "d2h_bytes_per_step": int(stats[4] / K), "wall_s": round(e2e_wall, 3),
@@ -269,6 +307,8 @@ def run_gb300(args, ws, rank, local, group):
         "gpu_launches": launches,
         "clocks": clk,
     }
+    if forms:
+        line["forms"] = forms
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
@@ -373,7 +413,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--interior", type=int, default=504, help="interior size n (n^3); 504 is the workload")
-    ap.add_argument("--form", default="fp32", choices=["fp32", "batch"])
+    ap.add_argument("--form", default="fp32", choices=["fp32", "fp16", "fp16x", "batch"])
+    ap.add_argument("--no-forms", action="store_true", help="skip timing the other storage forms")
+    ap.add_argument("--form-steps", type=int, default=200, help="timed steps of each other storage form")
     ap.add_argument("--shots", type=int, default=48)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-sequential", action="store_true")

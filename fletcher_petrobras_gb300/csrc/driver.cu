@@ -9,6 +9,9 @@
 //   coef        ten FP32 coefficient fields, [sz][10][sy][pitch], computed on
 //               the GPU in FP64 from the raw model arrays;
 //   scratch     one unpitched sx*sy*sz float volume for host transfers.
+// The 16-bit forms replace F by Hh[b] (half2 per cell) and, for FP16X, Hl[b]
+// (residual bytes), with per-plane exponents E (three fields: current,
+// previous, next) and per-plane maxima Mx (one per buffer).
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdarg.h>
@@ -49,6 +52,13 @@ struct State {
   long launches = 0;
   size_t dev_bytes = 0;
   int num_sms = 0;
+  int form = FLETCHER_FORM_FP32;
+  unsigned *Hh[2] = {nullptr, nullptr};
+  unsigned short *Hl[2] = {nullptr, nullptr};
+  int *E = nullptr;        // [3][sz] plane exponents, slot of the current field = ecur
+  unsigned *Mx = nullptr;  // [2][sz] plane maxima (float bits) of the field in buffer b
+  int ecur = 0;
+  HalfMaps hm[2];          // maps of a step whose current field is in buffer b
 };
 
 State g;
@@ -245,10 +255,13 @@ bool in_update_region(long idx) {
   return x >= g.bord && x < g.sx - g.bord && y >= g.bord && y < g.sy - g.bord && z >= g.bord && z < g.sz - g.bord;
 }
 
+bool half_form() { return g.form == FLETCHER_FORM_FP16 || g.form == FLETCHER_FORM_FP16X; }
+
 int check_err_word() {
-  if (g.err_host && *(volatile unsigned *)g.err_host)
-    return fail(FLETCHER_ERR_TIMEOUT, "a propagate kernel gave up waiting for its data (error word 0x%x)",
-                *(volatile unsigned *)g.err_host);
+  const unsigned w = g.err_host ? *(volatile unsigned *)g.err_host : 0u;
+  if (w & 3u)
+    return fail(FLETCHER_ERR_TIMEOUT, "a propagate kernel gave up waiting for its data (error word 0x%x)", w);
+  if (w & 4u) return fail(FLETCHER_ERR_RANGE, "a stored value exceeded FP16's range (error word 0x%x)", w);
   return FLETCHER_OK;
 }
 
@@ -257,6 +270,12 @@ void free_state() {
   if (g.F[1]) cudaFree(g.F[1]);
   if (g.coef) cudaFree(g.coef);
   if (g.scratch) cudaFree(g.scratch);
+  for (int b = 0; b < 2; ++b) {
+    if (g.Hh[b]) cudaFree(g.Hh[b]);
+    if (g.Hl[b]) cudaFree(g.Hl[b]);
+  }
+  if (g.E) cudaFree(g.E);
+  if (g.Mx) cudaFree(g.Mx);
   if (g.err_host) cudaFreeHost(g.err_host);
   g = State();
 }
@@ -281,7 +300,7 @@ int build_maps(ShotMaps *m, float2 *const F[2], float *coef, int sx, int sy, int
   const cuuint64_t str[2] = {(cuuint64_t)pitch * 8, (cuuint64_t)pitch * sy * 8};
   const cuuint32_t hbox[3] = {(cuuint32_t)(kTileX + 2 * kRadius), (cuuint32_t)(TY + 2 * kRadius), 1};
   const cuuint32_t pbox[3] = {(cuuint32_t)kTileX, (cuuint32_t)TY, 1};
-  for (int b = 0; b < 2; ++b) {
+  for (int b = 0; b < 2 && F[b]; ++b) {
     if (encode(&m->halo[b], CU_TENSOR_MAP_DATA_TYPE_INT64, 3, F[b], dims, str, hbox)) return g_last_err;
     if (encode(&m->pt[b], CU_TENSOR_MAP_DATA_TYPE_INT64, 3, F[b], dims, str, pbox)) return g_last_err;
   }
@@ -292,6 +311,33 @@ int build_maps(ShotMaps *m, float2 *const F[2], float *coef, int sx, int sy, int
   const cuuint32_t ubox[4] = {(cuuint32_t)kTileX, (cuuint32_t)TY, (cuuint32_t)kUpdateCoef, 1};
   if (encode(&m->arr, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, coef, cdims, cstr, abox)) return g_last_err;
   if (encode(&m->upd, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, coef, cdims, cstr, ubox)) return g_last_err;
+  return FLETCHER_OK;
+}
+
+// TMA descriptors of the 16-bit forms: for each choice of current buffer c,
+// the current field's halo boxes and the previous field's point boxes, plus
+// the coefficient boxes.
+int build_half_maps(HalfMaps hm[2], unsigned *const Hh[2], unsigned short *const Hl[2], const ShotMaps &fm, int sx,
+                    int sy, int sz, int pitch, int TY) {
+  const cuuint64_t dims[3] = {(cuuint64_t)sx, (cuuint64_t)sy, (cuuint64_t)sz};
+  const cuuint64_t sh[2] = {(cuuint64_t)pitch * 4, (cuuint64_t)pitch * sy * 4};
+  const cuuint64_t sl[2] = {(cuuint64_t)pitch * 2, (cuuint64_t)pitch * sy * 2};
+  const cuuint32_t hbox[3] = {(cuuint32_t)(kTileX + 2 * kRadius), (cuuint32_t)(TY + 2 * kRadius), 1};
+  const cuuint32_t pbox[3] = {(cuuint32_t)kTileX, (cuuint32_t)TY, 1};
+  const cuuint32_t lbox[3] = {(cuuint32_t)(kTileX + 2 * kRadius), (cuuint32_t)TY, 1};
+  for (int c = 0; c < 2; ++c) {
+    const int p = 1 - c;
+    HalfMaps &m = hm[c];
+    memset(&m, 0, sizeof(m));
+    if (encode(&m.cur_hi, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, Hh[c], dims, sh, hbox)) return g_last_err;
+    if (encode(&m.prev_hi, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, Hh[p], dims, sh, pbox)) return g_last_err;
+    if (Hl[c]) {
+      if (encode(&m.cur_lo, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, Hl[c], dims, sl, hbox)) return g_last_err;
+      if (encode(&m.prev_lo, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, Hl[p], dims, sl, lbox)) return g_last_err;
+    }
+    m.arr = fm.arr;
+    m.upd = fm.upd;
+  }
   return FLETCHER_OK;
 }
 
@@ -318,11 +364,31 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   if (!(dx > 0.f) || !(dy > 0.f) || !(dz > 0.f)) return fail(FLETCHER_ERR_ARGS, "grid spacing must be positive");
   if (!vpz || !vsv || !epsilon || !delta || !phi || !theta)
     return fail(FLETCHER_ERR_ARGS, "model arrays must not be NULL");
-  if (g_form != FLETCHER_FORM_FP32) return fail(FLETCHER_ERR_ARGS, "unknown storage form %d", g_form);
+  if (g_form < FLETCHER_FORM_FP32 || g_form > FLETCHER_FORM_FP16X)
+    return fail(FLETCHER_ERR_ARGS, "unknown storage form %d", g_form);
+  const bool half = g_form != FLETCHER_FORM_FP32;
+  const bool ext = g_form == FLETCHER_FORM_FP16X;
   const int rows = g_req_rows ? g_req_rows : 12;
   const int stages = g_req_stages ? g_req_stages : 5;
-  if (!propagate_fp32_supported(rows, stages))
-    return fail(FLETCHER_ERR_ARGS, "tile shape (%d rows, %d stages) is not built", rows, stages);
+  if (!(half ? propagate_half_supported(rows, stages) : propagate_fp32_supported(rows, stages)))
+    return fail(FLETCHER_ERR_ARGS, "tile shape (%d rows, %d stages) is not built for form %d", rows, stages, g_form);
+  if (half) {
+    // The 16-bit forms rescale every plane each step, so the cells that are
+    // never written must hold zero.
+    const float *f4[4] = {pp, pc, qp, qc};
+    for (int a = 0; a < 4; ++a) {
+      if (!f4[a]) continue;
+      for (long z = 0; z < sz; ++z)
+        for (long y = 0; y < sy; ++y) {
+          const bool inner = z >= bord && z < sz - bord && y >= bord && y < sy - bord;
+          for (long x = 0; x < sx; x = (inner && x == bord - 1) ? sx - bord : x + 1)
+            if (f4[a][(z * sy + y) * sx + x] != 0.0f)
+              return fail(FLETCHER_ERR_ARGS,
+                          "16-bit forms need zero initial fields outside the updated region (cell %ld)",
+                          (z * sy + y) * sx + x);
+        }
+    }
+  }
   if (ensure_stream()) return g_last_err;
 
   int dev = 0;
@@ -339,16 +405,34 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
 
   cudaStream_t s = g_stream;
 
-  CK(cudaMalloc(&g.F[0], g.npitch * sizeof(float2)));
-  CK(cudaMalloc(&g.F[1], g.npitch * sizeof(float2)));
+  g.form = g_form;
+  if (half) {
+    for (int b = 0; b < 2; ++b) {
+      CK(cudaMalloc(&g.Hh[b], g.npitch * sizeof(unsigned)));
+      CK(cudaMemsetAsync(g.Hh[b], 0, g.npitch * sizeof(unsigned), s));
+      if (ext) {
+        CK(cudaMalloc(&g.Hl[b], g.npitch * sizeof(unsigned short)));
+        CK(cudaMemsetAsync(g.Hl[b], 0, g.npitch * sizeof(unsigned short), s));
+      }
+    }
+    CK(cudaMalloc(&g.E, 3 * sz * sizeof(int)));
+    CK(cudaMalloc(&g.Mx, 2 * sz * sizeof(unsigned)));
+    CK(cudaMemsetAsync(g.E, 0, 3 * sz * sizeof(int), s));
+    CK(cudaMemsetAsync(g.Mx, 0, 2 * sz * sizeof(unsigned), s));
+    g.dev_bytes = 2 * g.npitch * (sizeof(unsigned) + (ext ? sizeof(unsigned short) : 0)) + 5 * sz * sizeof(int);
+  } else {
+    CK(cudaMalloc(&g.F[0], g.npitch * sizeof(float2)));
+    CK(cudaMalloc(&g.F[1], g.npitch * sizeof(float2)));
+    CK(cudaMemsetAsync(g.F[0], 0, g.npitch * sizeof(float2), s));
+    CK(cudaMemsetAsync(g.F[1], 0, g.npitch * sizeof(float2), s));
+    g.dev_bytes = 2 * g.npitch * sizeof(float2);
+  }
   CK(cudaMalloc(&g.coef, g.npitch * kNumCoef * sizeof(float)));
   CK(cudaMalloc(&g.scratch, g.n * sizeof(float)));
   CK(cudaHostAlloc(&g.err_host, sizeof(unsigned), cudaHostAllocMapped));
   *g.err_host = 0;
   CK(cudaHostGetDevicePointer((void **)&g.err_dev, g.err_host, 0));
-  g.dev_bytes = 2 * g.npitch * sizeof(float2) + g.npitch * kNumCoef * sizeof(float) + g.n * sizeof(float);
-  CK(cudaMemsetAsync(g.F[0], 0, g.npitch * sizeof(float2), s));
-  CK(cudaMemsetAsync(g.F[1], 0, g.npitch * sizeof(float2), s));
+  g.dev_bytes += g.npitch * kNumCoef * sizeof(float) + g.n * sizeof(float);
   CK(cudaMemsetAsync(g.coef, 0, g.npitch * kNumCoef * sizeof(float), s));
 
   // Raw model arrays -> coefficients (temporary 6-volume buffer).
@@ -362,13 +446,21 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   // Initial fields (the reference's OpenMP back-end works on the caller's
   // arrays, so their contents are the initial state).
   g.cur = 0;
+  g.ecur = 0;
   const float *fp[2][2] = {{pc, qc}, {pp, qp}};
   for (int b = 0; b < 2; ++b) {
     const float *p = fp[b][0], *q = fp[b][1];
     if (p) CK(cudaMemcpyAsync(raw, p, g.n * sizeof(float), cudaMemcpyHostToDevice, s));
     if (q) CK(cudaMemcpyAsync(raw + g.n, q, g.n * sizeof(float), cudaMemcpyHostToDevice, s));
-    k_pack<<<grid_for(g.n), 256, 0, s>>>(p ? raw : nullptr, q ? raw + g.n : nullptr, g.F[b], sx, sy, sz, g.pitch);
-    CK(cudaGetLastError());
+    if (half) {
+      // Buffer 0 holds the current field (exponent slot 0), buffer 1 the
+      // previous one (slot 2).
+      CK(half_encode(p ? raw : nullptr, q ? raw + g.n : nullptr, g.Hh[b], g.Hl[b], g.E + (b ? 2 : 0) * sz,
+                     g.Mx + b * sz, sx, sy, sz, g.pitch, ext, s));
+    } else {
+      k_pack<<<grid_for(g.n), 256, 0, s>>>(p ? raw : nullptr, q ? raw + g.n : nullptr, g.F[b], sx, sy, sz, g.pitch);
+      CK(cudaGetLastError());
+    }
   }
   CK(cudaStreamSynchronize(s));
   CK(cudaFree(raw));
@@ -376,6 +468,7 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   // Tensor maps and the shot descriptor.
   const int TY = rows;
   if (build_maps(&g.maps, g.F, g.coef, sx, sy, sz, g.pitch, TY)) return g_last_err;
+  if (half && build_half_maps(g.hm, g.Hh, g.Hl, g.maps, sx, sy, sz, g.pitch, TY)) return g_last_err;
   g.ntx = (sx - bord - kRadius + kTileX - 1) / kTileX;
   g.nty = (sy - bord - kRadius + TY - 1) / TY;
   const int ctas = g.num_sms * propagate_fp32_ctas_per_sm(TY);
@@ -452,7 +545,31 @@ int step() {
     want.cor_z = (int)(i / ((long)g.sx * g.sy));
     P.cor = g.owed.val;
   }
-  CK(propagate_fp32_launch(L, g_stream));
+  if (half_form()) {
+    const int enew = (g.ecur + 1) % 3, eprev = (g.ecur + 2) % 3;
+    const int sz = g.sz;
+    int sz_src = -1000;
+    if (fused) sz_src = want.src_z;
+    else if (g.owed.on) sz_src = want.cor_z;
+    const float sabs = fabsf(P.src) + fabsf(P.cor);
+    CK(half_scales(g.Mx + c * sz, g.Mx + p * sz, g.E + enew * sz, sz, sz_src, sabs, g_stream));
+    HalfLaunch HL;
+    HL.h.p = P;
+    HL.h.out_hi = g.Hh[p];
+    HL.h.out_lo = g.Hl[p];
+    HL.h.e_cur = g.E + g.ecur * sz;
+    HL.h.e_prev = g.E + eprev * sz;
+    HL.h.e_new = g.E + enew * sz;
+    HL.h.m_new = g.Mx + p * sz;
+    HL.m = g.hm[c];
+    HL.tile_rows = g.tile_rows;
+    HL.stages = g.stages;
+    HL.grid = g.grid;
+    CK(propagate_half_launch(HL, g.form == FLETCHER_FORM_FP16X, g_stream));
+    g.ecur = enew;
+  } else {
+    CK(propagate_fp32_launch(L, g_stream));
+  }
   ++g.launches;
   // The buffer that was current becomes the previous field; it lacks the
   // fused source, which the next step adds when it reads that cell.
@@ -462,9 +579,17 @@ int step() {
   return FLETCHER_OK;
 }
 
-int read_component(const float2 *F, int comp, float *host) {
-  k_unpack<<<grid_for(g.n), 256, 0, g_stream>>>(F, g.scratch, comp, g.sx, g.sy, g.sz, g.pitch);
-  CK(cudaGetLastError());
+// Component comp of buffer buf (which holds the current field when buf ==
+// g.cur) -> host.
+int read_component(int buf, int comp, float *host) {
+  if (half_form()) {
+    const int slot = buf == g.cur ? g.ecur : (g.ecur + 2) % 3;
+    CK(half_decode(g.Hh[buf], g.Hl[buf], g.E + slot * g.sz, g.scratch, comp, g.sx, g.sy, g.sz, g.pitch,
+                   g.form == FLETCHER_FORM_FP16X, grid_for(g.n), g_stream));
+  } else {
+    k_unpack<<<grid_for(g.n), 256, 0, g_stream>>>(g.F[buf], g.scratch, comp, g.sx, g.sy, g.sz, g.pitch);
+    CK(cudaGetLastError());
+  }
   CK(cudaMemcpyAsync(host, g.scratch, g.n * sizeof(float), cudaMemcpyDeviceToHost, g_stream));
   CK(cudaStreamSynchronize(g_stream));
   return check_err_word();
@@ -508,7 +633,7 @@ extern "C" void DRIVER_Propagate(const int sx, const int sy, const int sz, const
 
 extern "C" void DRIVER_Update_pointers(const int sx, const int sy, const int sz, float *pc) {
   if (check_dims(sx, sy, sz) || !pc) return;
-  if (read_component(g.F[g.cur], 0, pc)) return;
+  if (read_component(g.cur, 0, pc)) return;
   if (g.pending.on) pc[g.pending.idx] = pc[g.pending.idx] + g.pending.val;
 }
 
@@ -522,7 +647,15 @@ extern "C" void DRIVER_InsertSource(float dt, int it, int iSource, float *p, flo
     fail(FLETCHER_ERR_ARGS, "source index %d outside the grid", iSource);
     return;
   }
+  if (half_form() && !in_update_region(iSource)) {
+    fail(FLETCHER_ERR_ARGS, "16-bit forms need the source inside the updated region");
+    return;
+  }
   if (g.pending.on) {
+    if (half_form()) {
+      fail(FLETCHER_ERR_ARGS, "16-bit forms take one source per step");
+      return;
+    }
     // A second source before the next step: store the first one now.
     k_add_source<<<1, 32, 0, g_stream>>>(g.F[g.cur], pitched_index(g.pending.idx), g.pending.val);
     cudaError_t e = cudaGetLastError();
@@ -559,14 +692,16 @@ extern "C" int FLETCHER_SetStream(void *s) {
 extern "C" void *FLETCHER_GetStream(void) { return g_stream; }
 
 extern "C" int FLETCHER_SetForm(int form) {
-  if (form != FLETCHER_FORM_FP32) return fail(FLETCHER_ERR_ARGS, "unknown storage form %d", form);
+  if (form < FLETCHER_FORM_FP32 || form > FLETCHER_FORM_FP16X)
+    return fail(FLETCHER_ERR_ARGS, "unknown storage form %d", form);
   g_form = form;
   return FLETCHER_OK;
 }
 
 extern "C" int FLETCHER_SetTileConfig(int rows, int stages, int zchunks) {
   const int r = rows ? rows : 12, s = stages ? stages : 5;
-  if (!propagate_fp32_supported(r, s)) return fail(FLETCHER_ERR_ARGS, "tile shape (%d, %d) is not built", r, s);
+  if (!propagate_fp32_supported(r, s) && !propagate_half_supported(r, s))
+    return fail(FLETCHER_ERR_ARGS, "tile shape (%d, %d) is not built", r, s);
   if (zchunks < 0) return fail(FLETCHER_ERR_ARGS, "zchunks must be >= 0");
   g_req_rows = rows;
   g_req_stages = stages;
@@ -577,6 +712,8 @@ extern "C" int FLETCHER_SetTileConfig(int rows, int stages, int zchunks) {
 extern "C" int FLETCHER_Run(int nsteps, long iSource, const float *src) {
   if (!g.init) return fail(FLETCHER_ERR_ARGS, "FLETCHER_Run before DRIVER_Initialize");
   if (iSource >= 0 && ((size_t)iSource >= g.n || !src)) return fail(FLETCHER_ERR_ARGS, "bad source");
+  if (half_form() && iSource >= 0 && (!in_update_region(iSource) || g.pending.on))
+    return fail(FLETCHER_ERR_ARGS, "16-bit forms take one source per step inside the updated region");
   for (int s = 0; s < nsteps; ++s) {
     if (iSource >= 0) {
       if (g.pending.on) {
@@ -602,7 +739,7 @@ extern "C" int FLETCHER_GetField(int which, float *host) {
   if (!g.init) return fail(FLETCHER_ERR_ARGS, "FLETCHER_GetField before DRIVER_Initialize");
   if (which < 0 || which > 3 || !host) return fail(FLETCHER_ERR_ARGS, "bad field selector %d", which);
   const int buf = which < 2 ? g.cur : 1 - g.cur;
-  if (read_component(g.F[buf], which & 1, host)) return g_last_err;
+  if (read_component(buf, which & 1, host)) return g_last_err;
   const Source &fix = which < 2 ? g.pending : g.owed;
   if (fix.on) host[fix.idx] = host[fix.idx] + fix.val;
   return FLETCHER_OK;
@@ -624,8 +761,11 @@ extern "C" int FLETCHER_GetCoefficients(float *host) {
 extern "C" long FLETCHER_KernelLaunches(void) { return g.launches; }
 extern "C" size_t FLETCHER_DeviceBytes(void) { return g.dev_bytes; }
 extern "C" double FLETCHER_BytesPerCell(void) {
-  // current (p,q) 8 B + previous (p,q) 8 B + ten coefficients 40 B + next (p,q) 8 B.
-  return 64.0;
+  // current (p,q) + previous (p,q) + next (p,q) + ten FP32 coefficients (40 B):
+  // 8 B per field pair in FP32, 4 B in FP16, 6 B in FP16X.
+  const int form = g.init ? g.form : g_form;
+  const double pair = form == FLETCHER_FORM_FP16 ? 4.0 : (form == FLETCHER_FORM_FP16X ? 6.0 : 8.0);
+  return 3.0 * pair + 40.0;
 }
 
 // ===== Batched shots ==============================================================

@@ -79,6 +79,39 @@ int propagate_fp32_ctas_per_sm(int tile_rows);
 cudaError_t propagate_fp32_prepare(int tile_rows, int stages);
 cudaError_t propagate_fp32_launch(const PropLaunch &L, cudaStream_t s);
 
+// ---- 16-bit field storage (propagate_half.cu) ----
+// A field buffer holds (p, q) as half2 per cell ([z][y][pitch]) and, in the
+// extended form, one residual byte per value (a ushort per cell), with a
+// power-of-two scale per z-plane.
+struct HalfMaps {
+  CUtensorMap cur_hi, cur_lo;    // current field, halo box (TX+8, TY+8, 1)
+  CUtensorMap prev_hi, prev_lo;  // previous field: box (TX, TY, 1) / residuals (TX+8, TY, 1) from x0-4
+  CUtensorMap arr, upd;          // coefficients, as in the FP32 form
+};
+
+struct HalfParams {
+  PropParams p;                       // geometry (p.one), spacing, source, error word
+  unsigned *out_hi;                   // new field: half2 per cell
+  unsigned short *out_lo;             // new field: residual bytes (extended form)
+  const int *e_cur, *e_prev, *e_new;  // per-plane exponents of the current, previous and new field
+  unsigned *m_new;                    // per-plane max |value| of the new field (float bits), atomicMax
+};
+
+struct HalfLaunch {
+  HalfParams h;
+  HalfMaps m;
+  int tile_rows, stages, grid;
+};
+
+bool propagate_half_supported(int tile_rows, int stages);
+cudaError_t propagate_half_launch(const HalfLaunch &L, bool ext, cudaStream_t s);
+cudaError_t half_scales(const unsigned *m_cur, unsigned *m_prev, int *e_new, int sz, int src_z, float src_abs,
+                        cudaStream_t s);
+cudaError_t half_encode(const float *p, const float *q, unsigned *hv, unsigned short *rv, int *e, unsigned *m, int sx,
+                        int sy, int sz, int pitch, bool ext, cudaStream_t s);
+cudaError_t half_decode(const unsigned *hv, const unsigned short *rv, const int *e, float *out, int comp, int sx,
+                        int sy, int sz, int pitch, bool ext, int grid, cudaStream_t s);
+
 // Time limit of every device-side wait (ns).
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 

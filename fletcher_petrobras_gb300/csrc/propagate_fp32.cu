@@ -355,8 +355,11 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
           if (valid) out[(long)zc * plane] = nw.v;
         }
         if (!mbar_wait(xchg, xphase, kWaitLimitNs)) {
+          // A warp of this CTA stopped arriving (it gave up a wait itself):
+          // leave too, so that no thread keeps waiting step after step.
           *s_abort = 1;
           atomicOr(P.err, 2u);
+          goto aborted;
         }
         xphase ^= 1u;
         if (center) {

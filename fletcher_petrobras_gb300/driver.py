@@ -30,14 +30,28 @@ def _f32(a) -> np.ndarray:
     return a
 
 
-class Propagator:
-    """One resident simulation on the current GPU (the library holds one)."""
+# Storage forms of the wave fields (FLETCHER_FORM_*).
+FORMS = {"fp32": 0, "fp16": 1, "fp16x": 2}
 
-    def __init__(self, tile_rows: int = 0, stages: int = 0, zchunks: int = 0, stream: int | None = None):
+
+class Propagator:
+    """One resident simulation on the current GPU (the library holds one).
+
+    form: "fp32" (the reference's precision), "fp16" (FP16 fields with a
+    power-of-two scale per z-plane) or "fp16x" (FP16 plus a residual byte per
+    value); the arithmetic is FP32 in every form."""
+
+    def __init__(self, tile_rows: int = 0, stages: int = 0, zchunks: int = 0, stream: int | None = None,
+                 form: str = "fp32"):
         self.lib = _lib.load()
         self.lib.FLETCHER_ClearError()
         if stream is not None:
             self.lib.FLETCHER_SetStream(stream)
+        if form not in FORMS:
+            raise ValueError(f"unknown form {form!r}; one of {sorted(FORMS)}")
+        self.form = form
+        if self.lib.FLETCHER_SetForm(FORMS[form]):
+            _check(self.lib, "SetForm")
         if self.lib.FLETCHER_SetTileConfig(tile_rows, stages, zchunks):
             _check(self.lib, "SetTileConfig")
         self.shape = None

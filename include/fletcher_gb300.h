@@ -68,6 +68,7 @@ void DRIVER_InsertSource(float dt, int it, int iSource, float *p, float *q, floa
 #define FLETCHER_ERR_CUDA 2      /* a CUDA runtime call failed */
 #define FLETCHER_ERR_TIMEOUT 3   /* a kernel's bounded wait gave up */
 #define FLETCHER_ERR_NOMEM 4     /* device allocation failed */
+#define FLETCHER_ERR_RANGE 5     /* a 16-bit form's stored value left FP16's range */
 void FLETCHER_SetErrorMode(int mode);
 int FLETCHER_GetLastError(void);
 const char *FLETCHER_GetLastErrorString(void);
@@ -80,8 +81,18 @@ int FLETCHER_SetStream(void *cuda_stream);
 void *FLETCHER_GetStream(void);
 
 /* Storage form of the wave fields, chosen before DRIVER_Initialize.
- * FLETCHER_FORM_FP32: p,q in FP32 (the reference's precision). */
+ * FLETCHER_FORM_FP32: p,q in FP32 (the reference's precision).
+ * FLETCHER_FORM_FP16: p,q stored as FP16 with one power-of-two scale per
+ *   z-plane (set every step from the planes' largest magnitudes); the
+ *   arithmetic stays FP32.
+ * FLETCHER_FORM_FP16X: FP16 plus one residual byte per value (a 19-bit
+ *   significand, 3 bytes per value).
+ * The 16-bit forms keep every cell outside the updated region at zero:
+ * DRIVER_Initialize rejects initial fields that are not, and a source must
+ * lie inside the updated region, one per step. */
 #define FLETCHER_FORM_FP32 0
+#define FLETCHER_FORM_FP16 1
+#define FLETCHER_FORM_FP16X 2
 int FLETCHER_SetForm(int form);
 
 /* Kernel shape override for tuning (0 keeps the default): rows per tile,

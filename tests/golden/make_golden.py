@@ -8,6 +8,7 @@ the reference's RandomVelocityBoundary applied inside the reference build.
 
     python tests/golden/make_golden.py            # small cases (minutes)
     python tests/golden/make_golden.py --c1       # + the 504^3, 1000-step case (about an hour)
+    python tests/golden/make_golden.py --c2-f64   # FP64 oracle, 128^3 interior, 2000 steps (minutes)
 
 Each fixture stores the problem definition, hashes of the boundary-modified
 velocities and of the reference's coefficient fields, and the final current
@@ -149,11 +150,39 @@ def run_c1(stride: int = 12) -> None:
     print(f"wrote {out}")
 
 
+def run_c2_f64(stride: int = 4) -> None:
+    """The 128^3-interior layered case, 2000 steps, through the FP64 oracle
+    (the reference has no FP64 path; oracle/fletcher_oracle.c restates
+    original/sample.h in double with exact rational weights).  The error of
+    the 16-bit storage forms is measured against it."""
+    import oracle as orc
+    from fletcher_petrobras_gb300.models import C2
+
+    prob = C2
+    m = orc.boundary(prob.sx, prob.sy, prob.sz, prob.nx, prob.ny, prob.nz, prob.bord, prob.absorb,
+                     prob.raw_model(), prob.seed)
+    t0 = time.time()
+    p, q = orc.run_f64(prob, m)
+    print(f"  c2_f64: {prob.steps} steps on {prob.sx}x{prob.sy}x{prob.sz} in {time.time() - t0:.0f} s "
+          f"({orc.threads()} threads), max|p| {np.abs(p).max():.4g}")
+    meta = dataclasses.asdict(prob)
+    meta.update({"stride": stride, "precision": "f64", "vpz_sha": sha(m[0])})
+    out = os.path.join(HERE, "golden_c2_f64.npz")
+    np.savez_compressed(out, meta=np.array(json.dumps(meta)), p=subsample(p, prob, stride).astype(np.float32),
+                        q=subsample(q, prob, stride).astype(np.float32), psum=plane_sums(p, prob),
+                        qsum=plane_sums(q, prob))
+    print(f"wrote {out} ({os.path.getsize(out) / 1e3:.0f} kB)")
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--c1", action="store_true", help="also run the 504^3 x 1000-step case")
     ap.add_argument("--only-c1", action="store_true")
+    ap.add_argument("--c2-f64", action="store_true", help="only the FP64 oracle's 128^3, 2000-step case")
     a = ap.parse_args()
+    if a.c2_f64:
+        run_c2_f64()
+        return
     if not a.only_c1:
         lib = ref_lib()
         # Source values: the harness restates Source() for cut frequencies
