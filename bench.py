@@ -373,6 +373,65 @@ def run_batch_form(args, ws, rank, local, group):
     print(json.dumps(line), flush=True)
 
 
+def run_learned_form(args, ws, rank, local, group):
+    """C4: the learned 8-cell absorbing layer against the 32-cell random
+    shell, by default on a 256^3 interior for 1500 steps.  The network is
+    trained first (plain-method runs on 64 padded layered models, the
+    library's own training kernels); each form's interior MSamples/s is
+    timed with CUDA events and its reflected energy measured against a
+    wide-domain run."""
+    import math
+
+    import torch
+
+    from fletcher_petrobras_gb300 import learned
+
+    torch.cuda.set_device(local)
+    t0 = time.time()
+    ns = learned.collect(models=64, n_virtual=48, keep=0.1)
+    t1 = time.time()
+    learned.init(0)
+    loss = learned.train(iters=3000, batch=8192, lr=3e-3)
+    t2 = time.time()
+    n, steps = args.abc_interior, args.abc_steps
+    res = learned.compare(n=n, steps=steps, nsnap=5)
+    group.barrier()
+    if rank != 0:
+        return
+
+    def fin(v):
+        return v if isinstance(v, float) and math.isfinite(v) else None
+
+    forms = {}
+    for k, v in res.items():
+        if k == "snapshots":
+            continue
+        forms[k] = {"interior_msamples": round(v["interior_msamples"], 1), "ms_per_step": round(v["ms_per_step"], 4),
+                    "reflected_energy": fin(v["reflected_energy"]),
+                    "reflected_energy_by_snapshot": [fin(e) for e in v.get("reflected_energy_by_snapshot", [])],
+                    "launches_per_step": v.get("launches_per_step", 1)}
+    lv, rv = res["learned"], res["random"]
+    line = {
+        "metric": "interior MSamples/s, learned 8-cell layer vs 32-cell random boundary (C4)",
+        "value": round(lv["interior_msamples"], 1), "unit": UNIT, "n_gpus": ws, "steps": steps,
+        "higher_is_better": True, "scaling": "weak", "dtype": "f32 (network: f16 weights, f32 accumulation)",
+        "data": "synthetic (seeded layered TTI models)",
+        "config": {"workload": f"C4: {n}^3 interior, {steps} steps, dt 0.6 ms, 15 Hz Ricker 8 cells below the "
+                               "interior top; forms: learned 8-cell layer, 32-cell random-velocity shell, bare 8-cell "
+                               "layer (plain8), 8-cell taper (sponge), wide reflection-free reference",
+                   "snapshots": res["snapshots"],
+                   "training": {"models": 64, "samples": ns, "collect_s": round(t1 - t0, 1),
+                                "train_s": round(t2 - t1, 1), "iters": 3000, "batch": 8192,
+                                "loss_first": float(loss[:20].mean()), "loss_last": float(loss[-50:].mean())}},
+        "speedup_vs_random": round(rv["ms_per_step"] / lv["ms_per_step"], 3),
+        "reflected_energy_learned": fin(lv["reflected_energy"]),
+        "reflected_energy_random": fin(rv["reflected_energy"]),
+        "learned_stable": fin(lv["reflected_energy"]) is not None and lv["reflected_energy"] < 1.0,
+        "forms": forms,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, ws, rank, group):
     """The reference's CPU algorithm (its FP32 OpenMP loop, restated by the
     oracle) on the host cores, each step one propagation of a 16-plane slab
@@ -413,7 +472,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--interior", type=int, default=504, help="interior size n (n^3); 504 is the workload")
-    ap.add_argument("--form", default="fp32", choices=["fp32", "fp16", "fp16x", "batch"])
+    ap.add_argument("--form", default="fp32", choices=["fp32", "fp16", "fp16x", "batch", "learned"])
+    ap.add_argument("--abc-interior", type=int, default=256)
+    ap.add_argument("--abc-steps", type=int, default=1500)
     ap.add_argument("--no-forms", action="store_true", help="skip timing the other storage forms")
     ap.add_argument("--form-steps", type=int, default=200, help="timed steps of each other storage form")
     ap.add_argument("--shots", type=int, default=48)
@@ -429,6 +490,8 @@ def main():
             run_reference(args, ws, rank, group)
         elif args.form == "batch":
             run_batch_form(args, ws, rank, local, group)
+        elif args.form == "learned":
+            run_learned_form(args, ws, rank, local, group)
         else:
             run_gb300(args, ws, rank, local, group)
     finally:

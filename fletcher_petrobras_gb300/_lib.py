@@ -50,6 +50,19 @@ SIGNATURES = {
     "FLETCHER_RecommendedDt": (C.c_float, [C.c_long, FP, FP, C.c_float, C.c_float, C.c_float]),
     "FLETCHER_Model": (C.c_int, [C.c_int, C.c_long, C.c_double, C.c_float] + [C.c_int] * 4 + [C.c_float] * 4
                        + [FP] * 10 + [DP]),
+    "FLETCHER_AbcInit": (C.c_int, [C.c_uint]),
+    "FLETCHER_AbcSetWeights": (C.c_int, [FP, C.c_float]),
+    "FLETCHER_AbcGetWeights": (C.c_int, [FP, FP]),
+    "FLETCHER_AbcReserve": (C.c_int, [C.c_long]),
+    "FLETCHER_AbcCollect": (C.c_int, [IP, IP, C.c_int, C.c_float, C.c_uint, C.c_float]),
+    "FLETCHER_AbcSamples": (C.c_long, []),
+    "FLETCHER_AbcGetSamples": (C.c_int, [C.c_long, C.c_long, FP, FP, IP]),
+    "FLETCHER_AbcTrain": (C.c_int, [C.c_int, C.c_int, C.c_float, C.c_uint, C.c_float, FP]),
+    "FLETCHER_AbcGradient": (C.c_int, [FP, FP, C.c_int, FP, FP]),
+    "FLETCHER_AbcForward": (C.c_int, [FP, C.c_int, FP]),
+    "FLETCHER_SetBoundary": (C.c_int, [C.c_int, C.c_int, C.c_float]),
+    "FLETCHER_AbcLayerCells": (C.c_long, []),
+    "FLETCHER_AbcRelease": (None, []),
 }
 
 
@@ -79,3 +92,7 @@ def load(build_if_missing: bool = True):
 
 def fptr(a):
     return a.ctypes.data_as(FP) if a is not None else None
+
+
+def iptr(a):
+    return a.ctypes.data_as(IP) if a is not None else None

@@ -87,6 +87,23 @@ int fail(int code, const char *fmt, ...) {
 // status and error mode as the DRIVER_* entry points).
 int flt_record_error(int code, const char *msg) { return fail(code, "%s", msg); }
 
+namespace flt {
+ResidentView resident_view() {
+  ResidentView v;
+  v.init = g.init && g.form == FLETCHER_FORM_FP32;
+  if (!v.init) return v;
+  v.sx = g.sx; v.sy = g.sy; v.sz = g.sz; v.bord = g.bord; v.pitch = g.pitch;
+  v.dx = g.dx; v.dy = g.dy; v.dz = g.dz; v.dt = g.dt;
+  v.cur = g.F[g.cur];
+  v.prev = g.F[1 - g.cur];
+  v.next = g.F[1 - g.cur];
+  v.coef = g.coef;
+  v.stream = g_stream;
+  v.num_sms = g.num_sms;
+  return v;
+}
+}  // namespace flt
+
 namespace {
 
 #define CK(call)                                                                                   \
@@ -266,6 +283,7 @@ int check_err_word() {
 }
 
 void free_state() {
+  abc_release_resident();
   if (g.F[0]) cudaFree(g.F[0]);
   if (g.F[1]) cudaFree(g.F[1]);
   if (g.coef) cudaFree(g.coef);
@@ -568,7 +586,10 @@ int step() {
     CK(propagate_half_launch(HL, g.form == FLETCHER_FORM_FP16X, g_stream));
     g.ecur = enew;
   } else {
+    const bool abc = abc_active();
+    if (abc) CK(abc_before_step(resident_view()));
     CK(propagate_fp32_launch(L, g_stream));
+    if (abc) CK(abc_after_step(resident_view()));
   }
   ++g.launches;
   // The buffer that was current becomes the previous field; it lacks the

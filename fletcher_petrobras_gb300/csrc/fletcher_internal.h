@@ -112,6 +112,24 @@ cudaError_t half_encode(const float *p, const float *q, unsigned *hv, unsigned s
 cudaError_t half_decode(const unsigned *hv, const unsigned short *rv, const int *e, float *out, int comp, int sx,
                         int sy, int sz, int pitch, bool ext, int grid, cudaStream_t s);
 
+// ---- learned absorbing boundary (abc_learned.cu) ----
+// The resident single-shot state as the boundary layer sees it.
+struct ResidentView {
+  bool init = false;
+  int sx = 0, sy = 0, sz = 0, bord = 0, pitch = 0;
+  float dx = 0, dy = 0, dz = 0, dt = 0;
+  const float2 *cur = nullptr, *prev = nullptr;  // current and previous (p, q) fields (FP32 form)
+  float2 *next = nullptr;                        // the buffer the step writes
+  const float *coef = nullptr;                   // [z][10][y][pitch] (DevCoef order)
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+};
+ResidentView resident_view();       // driver.cu; cur/prev/next for the next step
+bool abc_active();                  // a learned layer is set on the resident state
+cudaError_t abc_before_step(const ResidentView &v);  // layer corrections from cur and prev
+cudaError_t abc_after_step(const ResidentView &v);   // adds them into next
+void abc_release_resident();        // the resident state is re-initialised or finalised
+
 // Time limit of every device-side wait (ns).
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 

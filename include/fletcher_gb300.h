@@ -233,6 +233,74 @@ int FLETCHER_Model(int st, long iSource, double fcut, float dt_output, int sx, i
                    float *qp, float *qc, float *vpz, float *vsv, float *epsilon, float *delta,
                    float *phi, float *theta, double *stats);
 
+/* ===== Part 4: learned absorbing boundary (no counterpart in the reference,
+ * whose absorbing zone is the random-velocity shell of original/boundary.c).
+ *
+ * The grid is interior + a layer of L cells + bord on every side, the medium
+ * extended into the layer.  The plain update covers interior and layer; the
+ * layer's face cells more than L - 4 cells outside the interior (whose
+ * stencils reach the zero border) get a correction from a per-cell MLP
+ * (40 -> 32 -> 32 -> 2, tanh, FP16 weights, FP32 accumulation) that predicts
+ * the update's contribution of an unbounded medium beyond the layer.
+ * Inputs: the 9-point outward-normal stencils of p and q at t and t-1
+ * (scaled by their largest magnitude s), vpz / 4000, epsilon, delta, d / L;
+ * the correction is s * out_scale * output.  FLETCHER_ABC_PARAMS master
+ * weights (FP32): W1 [32][40], b1 [32], W2 [32][32], b2 [32], W3 [2][32],
+ * b3 [2]. */
+#define FLETCHER_ABC_PARAMS 2434
+#define FLETCHER_BOUNDARY_PLAIN 0
+#define FLETCHER_BOUNDARY_LEARNED 1
+#define FLETCHER_BOUNDARY_SPONGE 2
+
+/* Network weights: random initialisation (Xavier, seeded), set, get. */
+int FLETCHER_AbcInit(unsigned seed);
+int FLETCHER_AbcSetWeights(const float *params, float out_scale);
+int FLETCHER_AbcGetWeights(float *params, float *out_scale);
+
+/* Training set on the device: AbcReserve(capacity) (re)allocates and
+ * empties it; AbcCollect appends samples from the resident FP32 state (its
+ * current and previous fields): around the interior box [lo, hi) with a
+ * layer of `layer` cells, a random fraction keep_frac of the network's layer
+ * cells whose stencil magnitude exceeds min_scale, each with its 40 inputs
+ * and target (the contribution of the cells beyond the layer to the cell's
+ * next p and q, over s).  The box, its layer and 4 more cells must lie in
+ * the updated region. */
+int FLETCHER_AbcReserve(long capacity);
+int FLETCHER_AbcCollect(const int *interior_lo, const int *interior_hi, int layer, float keep_frac, unsigned seed,
+                        float min_scale);
+long FLETCHER_AbcSamples(void);
+/* Samples [start, start + n): features [n][40], targets [n][2], and the
+ * cell of each (x, y, z, d: [n][4] ints); any pointer may be NULL. */
+int FLETCHER_AbcGetSamples(long start, long n, float *features, float *targets, int *cells);
+
+/* iters Adam steps (cosine-decayed learning rate from lr) on random batches
+ * of `batch` samples, the stencil inputs perturbed by noise of standard
+ * deviation `noise` (0: none); the first training of a set of weights fixes
+ * out_scale to the targets' root mean square.  loss_out: iters losses. */
+int FLETCHER_AbcTrain(int iters, int batch, float lr, unsigned seed, float noise, float *loss_out);
+
+/* One forward and backward pass on n given samples (features [n][40],
+ * targets [n][2], compared with the raw outputs): loss = sum (y - t)^2 /
+ * (2 n) and its gradient with respect to the master weights. */
+int FLETCHER_AbcGradient(const float *features, const float *targets, int n, float *grad, float *loss);
+
+/* The inference path (tensor cores) on n given feature rows: raw outputs
+ * [n][2]. */
+int FLETCHER_AbcForward(const float *features, int n, float *out);
+
+/* Boundary of the resident FP32 state.  FLETCHER_BOUNDARY_PLAIN: none.
+ * FLETCHER_BOUNDARY_LEARNED: a layer of `layer` cells (>= 5) inside the
+ * updated region (interior = updated region shrunk by `layer`) whose outer
+ * face cells get the network's correction; each step then also launches the
+ * layer's inference kernel (before the propagate kernel) and an add kernel
+ * (after it).  damping > 0 also scales every layer cell by exp(-(damping *
+ * d)^2) after the step.  FLETCHER_BOUNDARY_SPONGE: the same layer with that
+ * scaling only (damping > 0), no network.  FLETCHER_AbcLayerCells: cells
+ * the network evaluates per step. */
+int FLETCHER_SetBoundary(int mode, int layer, float damping);
+long FLETCHER_AbcLayerCells(void);
+void FLETCHER_AbcRelease(void);
+
 #ifdef __cplusplus
 }
 #endif
