@@ -50,6 +50,17 @@ SIGNATURES = {
     "FLETCHER_RecommendedDt": (C.c_float, [C.c_long, FP, FP, C.c_float, C.c_float, C.c_float]),
     "FLETCHER_Model": (C.c_int, [C.c_int, C.c_long, C.c_double, C.c_float] + [C.c_int] * 4 + [C.c_float] * 4
                        + [FP] * 10 + [DP]),
+    "FLETCHER_SnapshotBegin": (C.c_int, [C.c_int, FP]),
+    "FLETCHER_SnapshotWait": (C.c_int, []),
+    "FLETCHER_PinHost": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "FLETCHER_UnpinHost": (C.c_int, [C.c_void_p]),
+    "FLETCHER_DumpFieldToFile": (C.c_int, [C.c_int] * 9 + [C.c_float] * 3 + [FP, C.c_char_p]),
+    "FLETCHER_OpenSliceFile": (C.c_void_p, [C.c_int] * 6 + [C.c_float] * 4 + [C.c_char_p]),
+    "FLETCHER_DumpSliceFile": (C.c_int, [C.c_int] * 3 + [FP, C.c_void_p]),
+    "FLETCHER_SliceAppend": (C.c_int, [C.c_void_p, C.c_int]),
+    "FLETCHER_CloseSliceFile": (C.c_int, [C.c_void_p]),
+    "FLETCHER_SliceFrames": (C.c_int, [C.c_void_p]),
+    "FLETCHER_DumpSliceSummary": (C.c_int, [C.c_int] * 3 + [C.c_void_p, C.c_float, C.c_int, FP, C.c_float]),
     "FLETCHER_AbcInit": (C.c_int, [C.c_uint]),
     "FLETCHER_AbcSetWeights": (C.c_int, [FP, C.c_float]),
     "FLETCHER_AbcGetWeights": (C.c_int, [FP, FP]),

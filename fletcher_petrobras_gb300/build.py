@@ -26,7 +26,7 @@ NVCC_FLAGS = GENCODE + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-
 CC = os.environ.get("CC", "gcc")
 C_FLAGS = ["-O3", "-fPIC", "-ffp-contract=off", "-std=gnu11", "-Wall", "-I" + INCLUDE]
 
-CU_SOURCES = ["driver.cu", "propagate_fp32.cu", "propagate_half.cu", "abc_learned.cu", "noalloc.cu"]
+CU_SOURCES = ["driver.cu", "propagate_fp32.cu", "propagate_half.cu", "abc_learned.cu", "snapshot.cu", "noalloc.cu"]
 C_SOURCES = ["host/fletcher_host.c"]
 HEADERS = ["device_util.cuh", "fletcher_internal.h", "stencil_common.cuh"]
 

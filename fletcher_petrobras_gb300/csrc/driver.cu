@@ -284,6 +284,7 @@ int check_err_word() {
 
 void free_state() {
   abc_release_resident();
+  snapshot_release();
   if (g.F[0]) cudaFree(g.F[0]);
   if (g.F[1]) cudaFree(g.F[1]);
   if (g.coef) cudaFree(g.coef);
@@ -619,6 +620,35 @@ int read_component(int buf, int comp, float *host) {
 }  // namespace
 
 // ===== Part 1 ====================================================================
+
+namespace flt {
+int resident_field_to_device(int which, float *dev_out, long *fix_idx, float *fix_val) {
+  if (!g.init) return fail(FLETCHER_ERR_ARGS, "no resident state");
+  if (which < 0 || which > 3) return fail(FLETCHER_ERR_ARGS, "bad field selector %d", which);
+  const int buf = which < 2 ? g.cur : 1 - g.cur, comp = which & 1;
+  if (half_form()) {
+    const int slot = buf == g.cur ? g.ecur : (g.ecur + 2) % 3;
+    CK(half_decode(g.Hh[buf], g.Hl[buf], g.E + slot * g.sz, dev_out, comp, g.sx, g.sy, g.sz, g.pitch,
+                   g.form == FLETCHER_FORM_FP16X, grid_for(g.n), g_stream));
+  } else {
+    k_unpack<<<grid_for(g.n), 256, 0, g_stream>>>(g.F[buf], dev_out, comp, g.sx, g.sy, g.sz, g.pitch);
+    CK(cudaGetLastError());
+  }
+  const Source &fix = which < 2 ? g.pending : g.owed;
+  *fix_idx = fix.on ? fix.idx : -1;
+  *fix_val = fix.on ? fix.val : 0.f;
+  return FLETCHER_OK;
+}
+size_t resident_cells() { return g.init ? g.n : 0; }
+bool resident_dims(int *sx, int *sy, int *sz) {
+  if (!g.init) return false;
+  *sx = g.sx;
+  *sy = g.sy;
+  *sz = g.sz;
+  return true;
+}
+cudaStream_t resident_stream() { return g_stream; }
+}  // namespace flt
 
 extern "C" void DRIVER_Initialize(const int sx, const int sy, const int sz, const int bord, float dx, float dy,
                                   float dz, float dt, float *vpz, float *vsv, float *epsilon, float *delta,

@@ -130,6 +130,17 @@ cudaError_t abc_before_step(const ResidentView &v);  // layer corrections from c
 cudaError_t abc_after_step(const ResidentView &v);   // adds them into next
 void abc_release_resident();        // the resident state is re-initialised or finalised
 
+// ---- output path (snapshot.cu) ----
+// Field `which` (0 current p, 1 current q, 2 previous p, 3 previous q) of the
+// resident state, any storage form, as an unpitched FP32 volume in dev_out,
+// issued on the library's stream.  fix_idx / fix_val: the one cell whose
+// stored value lacks a source addition the interface shows (-1: none).
+int resident_field_to_device(int which, float *dev_out, long *fix_idx, float *fix_val);
+size_t resident_cells();             // sx * sy * sz (0 when not initialised)
+bool resident_dims(int *sx, int *sy, int *sz);  // grid of the resident state (any form)
+cudaStream_t resident_stream();      // the library's stream
+void snapshot_release();             // driver.cu calls it when the state goes away
+
 // Time limit of every device-side wait (ns).
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 

@@ -187,6 +187,11 @@ int FLETCHER_Model(int st, long iSource, double fcut, float dt_output, int sx, i
                     pc, qp, qc);
   if (FLETCHER_GetLastError()) return FLETCHER_GetLastError();
   double h2d = 10.0 * n * sizeof(float), d2h = 0.0;
+  /* Snapshots go straight into the two host p arrays (page-locked for the
+   * call) while the steps continue. */
+  const int pinned = dt_output > 0.0f && !FLETCHER_PinHost(pp, n * sizeof(float)) &&
+                     !FLETCHER_PinHost(pc, n * sizeof(float));
+  if (dt_output > 0.0f && !pinned) FLETCHER_ClearError();
   double walltime = 0.0;
   float tSim = 0.0;
   int nOut = 1;
@@ -199,13 +204,24 @@ int FLETCHER_Model(int st, long iSource, double fcut, float dt_output, int sx, i
     float *t = pp; pp = pc; pc = t;
     t = qp; qp = qc; qc = t;
     walltime += wall_seconds() - t0;
-    if (FLETCHER_GetLastError()) return FLETCHER_GetLastError();
+    if (FLETCHER_GetLastError()) break;
     tSim = it * dt;
     if (dt_output > 0.0f && tSim >= tOut) {
-      DRIVER_Update_pointers(sx, sy, sz, pc);
+      /* DRIVER_Update_pointers(pc) of original/model.c:100, without waiting. */
+      if (FLETCHER_SnapshotBegin(0, pc)) break;
       d2h += (double)n * sizeof(float);
       tOut = (++nOut) * dt_output;
     }
+  }
+  FLETCHER_SnapshotWait();
+  if (pinned) {
+    FLETCHER_UnpinHost(pp);
+    FLETCHER_UnpinHost(pc);
+  }
+  if (FLETCHER_GetLastError()) {
+    const int e = FLETCHER_GetLastError();
+    DRIVER_Finalize();
+    return e;
   }
   int rc = FLETCHER_GetField(0, pc0);
   if (!rc) rc = FLETCHER_GetField(1, qc0);

@@ -129,6 +129,44 @@ size_t FLETCHER_DeviceBytes(void);
  * next field). */
 double FLETCHER_BytesPerCell(void);
 
+/* ---- Output path (original/utils.c:7-227, original/model.c:98-107).
+ *
+ * Snapshots: FLETCHER_SnapshotBegin(which, host) starts copying field
+ * `which` (0 current p, 1 current q, 2 previous p, 3 previous q; any storage
+ * form, decoded to FP32) of the resident state into `host` (sx*sy*sz
+ * floats) and returns at once: the copy is ordered after the steps issued so
+ * far and overlaps the steps issued after it.  FLETCHER_SnapshotWait()
+ * waits for the snapshots started so far.  A page-locked destination
+ * (FLETCHER_PinHost, cudaHostAlloc) is written by the copy engine directly;
+ * any other buffer through a page-locked staging buffer.  The destination
+ * must not be touched until FLETCHER_SnapshotWait returns. */
+int FLETCHER_SnapshotBegin(int which, float *host);
+int FLETCHER_SnapshotWait(void);
+int FLETCHER_PinHost(void *ptr, size_t bytes);
+int FLETCHER_UnpinHost(void *ptr);
+
+/* RSF (Madagascar) files with the reference's names and layout: a text
+ * header <fName>.rsf and a binary <fName>.rsf@ of native floats, x fastest.
+ * Boxes are inclusive grid indices [ixStart, ixEnd] x ... as in the
+ * reference.  DumpFieldToFile writes one box of a host array
+ * (original/utils.c:7-52).  A slice file (OpenSliceFile, :66-120) is
+ * appended to from a host array (DumpSliceFile, :126-146) or, without
+ * blocking, from the resident state (SliceAppend: the box is gathered on
+ * the device and written by a host callback after its copy); CloseSliceFile
+ * (:152-198) waits for pending appends and writes the header with the
+ * frame count.  DumpSliceSummary (:204-224) prints the box's extrema. */
+typedef struct FletcherSlice FletcherSlice;
+int FLETCHER_DumpFieldToFile(int sx, int sy, int sz, int ixStart, int ixEnd, int iyStart, int iyEnd, int izStart,
+                             int izEnd, float d1, float d2, float d3, const float *arr, const char *fName);
+FletcherSlice *FLETCHER_OpenSliceFile(int ixStart, int ixEnd, int iyStart, int iyEnd, int izStart, int izEnd,
+                                      float dx, float dy, float dz, float dt, const char *fName);
+int FLETCHER_DumpSliceFile(int sx, int sy, int sz, const float *arr, FletcherSlice *slice);
+int FLETCHER_SliceAppend(FletcherSlice *slice, int which);
+int FLETCHER_CloseSliceFile(FletcherSlice *slice);
+int FLETCHER_SliceFrames(const FletcherSlice *slice);
+int FLETCHER_DumpSliceSummary(int sx, int sy, int sz, const FletcherSlice *slice, float dt, int it,
+                              const float *arr, float src);
+
 /* ---- Batched shots (no counterpart in the reference, whose runs are one
  * shot per process).  Independent shots of different sizes share one
  * persistent launch per time step; the time loop runs as one CUDA graph.
@@ -222,7 +260,9 @@ float FLETCHER_RecommendedDt(long n, const float *vpz, const float *epsilon, flo
  * source for time (it-1)*dt, DRIVER_Propagate and the pointer swap (the
  * timed region, as original/model.c:82-88), and DRIVER_Update_pointers of
  * the current p every dt_output seconds of simulated time (dt_output <= 0:
- * never).  The final current p and q are copied to pc and qc, and
+ * never; the snapshots are asynchronous and land in the host array the
+ * reference's loop would name pc at that step -- both host p arrays are
+ * page-locked for the call).  The final current p and q are copied to pc and qc, and
  * DRIVER_Finalize is called.  Results in stats (may be NULL):
  * stats[0] = propagate wall seconds, stats[1] = MSamples/s by the
  * reference's definition, stats[2] = whole-call wall seconds, stats[3] =

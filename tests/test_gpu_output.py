@@ -1,0 +1,108 @@
+"""Asynchronous output path on the GPU, through the C ABI: snapshots and
+slice appends taken while steps keep running must equal the synchronous
+read-back (FLETCHER_GetField) of the same step, bit for bit, in the FP32
+and FP16X forms, into page-locked and ordinary host buffers."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import gpu_available
+from fletcher_petrobras_gb300 import Problem, Propagator
+from fletcher_petrobras_gb300._lib import fptr
+
+pytestmark = pytest.mark.gpu
+
+PROB = Problem("snap", 40, 30, 24, absorb=5, dt=0.0006, steps=40, fcut=45.0, kind="layered", layers=3, seed=8)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not gpu_available():
+        pytest.fail("these tests need a CUDA GPU")
+
+
+def start(form):
+    prop = Propagator(form=form)
+    p = PROB
+    prop.initialize(p.sx, p.sy, p.sz, p.bord, p.dx, p.dy, p.dz, p.dt, p.model())
+    return prop
+
+
+@pytest.mark.parametrize("form", ["fp32", "fp16x"])
+@pytest.mark.parametrize("pinned", [False, True])
+def test_snapshot_equals_field_of_its_step(form, pinned):
+    prop = start(form)
+    lib = prop.lib
+    src = PROB.sources()
+    prop.run(20, PROB.i_source, src[:20])
+    n = PROB.n
+    outs = [np.full(n, np.nan, np.float32) for _ in range(4)]
+    if pinned:
+        for o in outs:
+            assert lib.FLETCHER_PinHost(o.ctypes.data, o.nbytes) == 0
+    for k in range(4):
+        assert lib.FLETCHER_SnapshotBegin(k, fptr(outs[k])) == 0
+    prop.run(20, PROB.i_source, src[20:])  # overlaps the copies
+    assert lib.FLETCHER_SnapshotWait() == 0
+    after = [prop.field(k) for k in range(4)]
+    prop.finalize()
+    # the same state, run to step 20 only
+    prop = start(form)
+    prop.run(20, PROB.i_source, src[:20])
+    want = [prop.field(k) for k in range(4)]
+    prop.finalize()
+    Propagator(form="fp32")
+    if pinned:
+        for o in outs:
+            lib.FLETCHER_UnpinHost(o.ctypes.data)
+    for k in range(4):
+        assert np.array_equal(outs[k], want[k]), k
+        assert not np.array_equal(outs[k], after[k])
+
+
+def test_slice_append_equals_host_slice_file(tmp_path, monkeypatch):
+    prop = start("fp32")
+    lib = prop.lib
+    p = PROB
+    monkeypatch.chdir(tmp_path)
+    box = (4, p.sx - 5, p.sy // 2, p.sy // 2, 4, p.sz - 5)  # a y-slice
+    a = lib.FLETCHER_OpenSliceFile(*box, p.dx, p.dz, p.dz, p.dt, b"async")
+    h = lib.FLETCHER_OpenSliceFile(*box, p.dx, p.dz, p.dz, p.dt, b"host")
+    src = p.sources()
+    for it in range(0, 40, 10):
+        prop.run(10, p.i_source, src[it:it + 10])
+        assert lib.FLETCHER_SliceAppend(a, 0) == 0
+        f = prop.field(0)
+        assert lib.FLETCHER_DumpSliceFile(p.sx, p.sy, p.sz, fptr(f), h) == 0
+    assert lib.FLETCHER_CloseSliceFile(a) == 0 and lib.FLETCHER_CloseSliceFile(h) == 0
+    prop.finalize()
+    for ext in (".rsf", ".rsf@"):
+        x = open(os.path.join(tmp_path, "async" + ext), "rb").read()
+        y = open(os.path.join(tmp_path, "host" + ext), "rb").read()
+        assert x.replace(b"async", b"host") == y, ext
+    assert os.path.getsize(os.path.join(tmp_path, "host.rsf@")) == 4 * 4 * (box[1] - box[0] + 1) * (box[5] - box[4] + 1)
+
+
+def test_model_loop_snapshots_land_in_the_callers_arrays():
+    """FLETCHER_Model with a snapshot cadence: the asynchronous snapshots
+    leave the last one in a host p array and the final fields in pc / qc."""
+    import ctypes as C
+
+    p = PROB
+    prop = Propagator()
+    lib = prop.lib
+    m = p.model()
+    f = np.zeros((4, p.n), np.float32)
+    stats = (C.c_double * 5)()
+    rc = lib.FLETCHER_Model(p.steps, p.i_source, p.fcut, 0.003, p.sx, p.sy, p.sz, p.bord, p.dx, p.dy, p.dz, p.dt,
+                            *[fptr(f[k]) for k in range(4)], *[fptr(m[k]) for k in range(6)], stats)
+    assert rc == 0
+    prop2 = Propagator()
+    prop2.initialize(p.sx, p.sy, p.sz, p.bord, p.dx, p.dy, p.dz, p.dt, m)
+    src = p.sources()
+    prop2.run(p.steps, p.i_source, src)
+    want_p, want_q = prop2.field(0), prop2.field(1)
+    prop2.finalize()
+    assert np.array_equal(f[1], want_p) and np.array_equal(f[3], want_q)
+    assert stats[4] > 2 * 4 * p.n  # snapshots were taken
