@@ -50,6 +50,10 @@ SIGNATURES = {
     "FLETCHER_RecommendedDt": (C.c_float, [C.c_long, FP, FP, C.c_float, C.c_float, C.c_float]),
     "FLETCHER_Model": (C.c_int, [C.c_int, C.c_long, C.c_double, C.c_float] + [C.c_int] * 4 + [C.c_float] * 4
                        + [FP] * 10 + [DP]),
+    "FLETCHER_Autotune": (C.c_int, [C.c_char_p, C.c_int]),
+    "FLETCHER_GetTileConfig": (C.c_int, [IP, IP]),
+    "FLETCHER_TuneConfigLookup": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_int, IP, IP]),
+    "FLETCHER_TuneConfigStore": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int]),
     "FLETCHER_SnapshotBegin": (C.c_int, [C.c_int, FP]),
     "FLETCHER_SnapshotWait": (C.c_int, []),
     "FLETCHER_PinHost": (C.c_int, [C.c_void_p, C.c_size_t]),

@@ -19,6 +19,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <vector>
+
 #include "../../include/fletcher_gb300.h"
 #include "fletcher_internal.h"
 
@@ -62,6 +64,20 @@ struct State {
 };
 
 State g;
+
+// Online tile-shape tuning (FLETCHER_Autotune): each candidate shape runs
+// `per_shape` timed steps after one warm-up step; the steps are real steps.
+struct Tuner {
+  bool active = false;
+  char path[512] = "";
+  int per_shape = 0;
+  std::vector<int> rows, stages;
+  std::vector<float> ms;
+  size_t idx = 0;
+  int left = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+};
+Tuner tune;
 cudaStream_t g_stream = nullptr;
 bool g_own_stream = false;
 int g_form = FLETCHER_FORM_FP32;
@@ -283,6 +299,7 @@ int check_err_word() {
 }
 
 void free_state() {
+  tune.active = false;
   abc_release_resident();
   snapshot_release();
   if (g.F[0]) cudaFree(g.F[0]);
@@ -372,6 +389,30 @@ void fill_items(int4 *items, int shot, int ntx, int nty, int nchunk, int TY) {
 }  // namespace flt
 
 namespace {
+
+// Tensor maps, work items and the shot descriptor for a tile shape (at
+// initialisation, or between steps: results do not depend on the shape).
+int setup_tiles(int rows, int stages) {
+  const int TY = rows, sx = g.sx, sy = g.sy, sz = g.sz, bord = g.bord;
+  if (build_maps(&g.maps, g.F, g.coef, sx, sy, sz, g.pitch, TY)) return g_last_err;
+  if (half_form() && build_half_maps(g.hm, g.Hh, g.Hl, g.maps, sx, sy, sz, g.pitch, TY)) return g_last_err;
+  g.tile_rows = rows;
+  g.stages = stages;
+  g.ntx = (sx - bord - kRadius + kTileX - 1) / kTileX;
+  g.nty = (sy - bord - kRadius + TY - 1) / TY;
+  const int ctas = g.num_sms * propagate_fp32_ctas_per_sm(TY);
+  choose_chunks(ctas, g.ntx * g.nty, sz - 2 * bord, g.zchunks, &g.nchunk, &g.chunk);
+  g.nitems = g.ntx * g.nty * g.nchunk;
+  g.grid = g.nitems < ctas ? g.nitems : ctas;
+  memset(&g.desc, 0, sizeof(g.desc));
+  g.desc.F[0] = g.F[0];
+  g.desc.F[1] = g.F[1];
+  g.desc.sx = sx; g.desc.sy = sy; g.desc.sz = sz; g.desc.pitch = g.pitch; g.desc.bord = bord;
+  g.desc.ntx = g.ntx; g.desc.nty = g.nty; g.desc.chunk = g.chunk;
+  g.desc.src_x = g.desc.src_y = g.desc.src_z = -1000;
+  g.desc.cor_x = g.desc.cor_y = g.desc.cor_z = -1000;
+  return FLETCHER_OK;
+}
 
 int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, float dt, const float *vpz,
                const float *vsv, const float *epsilon, const float *delta, const float *phi, const float *theta,
@@ -484,23 +525,7 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   CK(cudaStreamSynchronize(s));
   CK(cudaFree(raw));
 
-  // Tensor maps and the shot descriptor.
-  const int TY = rows;
-  if (build_maps(&g.maps, g.F, g.coef, sx, sy, sz, g.pitch, TY)) return g_last_err;
-  if (half && build_half_maps(g.hm, g.Hh, g.Hl, g.maps, sx, sy, sz, g.pitch, TY)) return g_last_err;
-  g.ntx = (sx - bord - kRadius + kTileX - 1) / kTileX;
-  g.nty = (sy - bord - kRadius + TY - 1) / TY;
-  const int ctas = g.num_sms * propagate_fp32_ctas_per_sm(TY);
-  choose_chunks(ctas, g.ntx * g.nty, sz - 2 * bord, g.zchunks, &g.nchunk, &g.chunk);
-  g.nitems = g.ntx * g.nty * g.nchunk;
-  g.grid = g.nitems < ctas ? g.nitems : ctas;
-  memset(&g.desc, 0, sizeof(g.desc));
-  g.desc.F[0] = g.F[0];
-  g.desc.F[1] = g.F[1];
-  g.desc.sx = sx; g.desc.sy = sy; g.desc.sz = sz; g.desc.pitch = g.pitch; g.desc.bord = bord;
-  g.desc.ntx = g.ntx; g.desc.nty = g.nty; g.desc.chunk = g.chunk;
-  g.desc.src_x = g.desc.src_y = g.desc.src_z = -1000;
-  g.desc.cor_x = g.desc.cor_y = g.desc.cor_z = -1000;
+  if (setup_tiles(rows, stages)) return g_last_err;
   g.launches = 0;
   g.pending = Source();
   g.owed = Source();
@@ -508,8 +533,42 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   return FLETCHER_OK;
 }
 
+const char *form_name(int form) {
+  return form == FLETCHER_FORM_FP16 ? "fp16" : (form == FLETCHER_FORM_FP16X ? "fp16x" : "fp32");
+}
+
+int tune_before_step() {
+  if (tune.left == 0) {
+    if (setup_tiles(tune.rows[tune.idx], tune.stages[tune.idx])) return g_last_err;
+    tune.left = tune.per_shape + 1;
+  }
+  if (tune.left == tune.per_shape) CK(cudaEventRecord(tune.e0, g_stream));
+  return FLETCHER_OK;
+}
+
+int tune_after_step() {
+  if (--tune.left > 0) return FLETCHER_OK;
+  CK(cudaEventRecord(tune.e1, g_stream));
+  CK(cudaEventSynchronize(tune.e1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, tune.e0, tune.e1));
+  tune.ms.push_back(ms / tune.per_shape);
+  if (++tune.idx < tune.rows.size()) return FLETCHER_OK;
+  size_t best = 0;
+  for (size_t i = 1; i < tune.ms.size(); ++i)
+    if (tune.ms[i] < tune.ms[best]) best = i;
+  tune.active = false;
+  if (setup_tiles(tune.rows[best], tune.stages[best])) return g_last_err;
+  cudaDeviceProp prop;
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaGetDeviceProperties(&prop, dev));
+  return FLETCHER_TuneConfigStore(tune.path, prop.name, g.sx, g.form, tune.rows[best], tune.stages[best]);
+}
+
 // One step: source `pending` (if any) fused, then rotation.
 int step() {
+  if (tune.active && tune_before_step()) return g_last_err;
   PropLaunch L;
   const int c = g.cur, p = 1 - g.cur;
   L.tile_rows = g.tile_rows;
@@ -593,6 +652,7 @@ int step() {
     if (abc) CK(abc_after_step(resident_view()));
   }
   ++g.launches;
+  if (tune.active && tune_after_step()) return g_last_err;
   // The buffer that was current becomes the previous field; it lacks the
   // fused source, which the next step adds when it reads that cell.
   g.owed = fused ? g.pending : Source();
@@ -817,6 +877,82 @@ extern "C" double FLETCHER_BytesPerCell(void) {
   const int form = g.init ? g.form : g_form;
   const double pair = form == FLETCHER_FORM_FP16 ? 4.0 : (form == FLETCHER_FORM_FP16X ? 6.0 : 8.0);
   return 3.0 * pair + 40.0;
+}
+
+// ---- tile-shape tuning with a configuration file --------------------------------
+
+extern "C" int FLETCHER_TuneConfigLookup(const char *path, const char *gpu, int sx, int form, int *rows,
+                                         int *stages) {
+  if (!path || !gpu || !rows || !stages) return fail(FLETCHER_ERR_ARGS, "TuneConfigLookup: bad arguments");
+  FILE *f = fopen(path, "r");
+  if (!f) return 0;
+  char line[512];
+  int found = 0;
+  while (fgets(line, sizeof(line), f)) {
+    char name[128], fname[16];
+    int ssx, bx, by, st;
+    // The reference's four fields first (original_singleGPU_PDP/model.c:81), then ours.
+    if (sscanf(line, "%127[^|] | %d | %d | %d | %d | %15s", name, &ssx, &bx, &by, &st, fname) != 6) continue;
+    size_t L = strlen(name);
+    while (L && (name[L - 1] == ' ' || name[L - 1] == '\t')) name[--L] = 0;
+    if (strcmp(name, gpu) || ssx != sx || bx != kTileX || strcmp(fname, form_name(form))) continue;
+    const bool ok = form == FLETCHER_FORM_FP32 ? propagate_fp32_supported(by, st) : propagate_half_supported(by, st);
+    if (!ok) continue;
+    *rows = by;
+    *stages = st;
+    found = 1;  // the last matching line wins
+  }
+  fclose(f);
+  return found;
+}
+
+extern "C" int FLETCHER_TuneConfigStore(const char *path, const char *gpu, int sx, int form, int rows, int stages) {
+  if (!path || !gpu) return fail(FLETCHER_ERR_ARGS, "TuneConfigStore: bad arguments");
+  FILE *f = fopen(path, "a");
+  if (!f) return fail(FLETCHER_ERR_ARGS, "TuneConfigStore: cannot open %s", path);
+  fprintf(f, "%s | %d | %d | %d | %d | %s\n", gpu, sx, kTileX, rows, stages, form_name(form));
+  fclose(f);
+  return FLETCHER_OK;
+}
+
+extern "C" int FLETCHER_Autotune(const char *path, int steps_per_shape) {
+  if (!g.init) return fail(FLETCHER_ERR_ARGS, "FLETCHER_Autotune before DRIVER_Initialize");
+  if (!path || strlen(path) >= sizeof(tune.path) || steps_per_shape < 1)
+    return fail(FLETCHER_ERR_ARGS, "FLETCHER_Autotune: bad arguments");
+  cudaDeviceProp prop;
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaGetDeviceProperties(&prop, dev));
+  int rows = 0, stages = 0;
+  const int found = FLETCHER_TuneConfigLookup(path, prop.name, g.sx, g.form, &rows, &stages);
+  if (found < 0) return g_last_err;
+  if (found) {
+    tune.active = false;
+    if (setup_tiles(rows, stages)) return g_last_err;
+    return 1;
+  }
+  tune = Tuner();
+  strcpy(tune.path, path);
+  tune.per_shape = steps_per_shape;
+  static const int cand[][2] = {{12, 4}, {12, 5}, {12, 6}, {16, 5}, {8, 5}, {8, 6}};
+  for (const auto &c : cand) {
+    const bool ok = half_form() ? propagate_half_supported(c[0], c[1]) : propagate_fp32_supported(c[0], c[1]);
+    if (ok) {
+      tune.rows.push_back(c[0]);
+      tune.stages.push_back(c[1]);
+    }
+  }
+  CK(cudaEventCreate(&tune.e0));
+  CK(cudaEventCreate(&tune.e1));
+  tune.active = true;
+  return 0;
+}
+
+extern "C" int FLETCHER_GetTileConfig(int *rows, int *stages) {
+  if (!g.init) return fail(FLETCHER_ERR_ARGS, "FLETCHER_GetTileConfig before DRIVER_Initialize");
+  if (rows) *rows = g.tile_rows;
+  if (stages) *stages = g.stages;
+  return tune.active ? 1 : 0;
 }
 
 // ===== Batched shots ==============================================================

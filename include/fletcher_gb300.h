@@ -99,6 +99,25 @@ int FLETCHER_SetForm(int form);
  * pipeline stages, z-chunks per column. */
 int FLETCHER_SetTileConfig(int tile_rows, int stages, int zchunks);
 
+/* Tile-shape tuning with a configuration file in the format of the
+ * reference's block-size tuner (original_singleGPU_PDP/model.c:51-113,
+ * lines "<GPU name> | <sx> | <bsize_x> | <bsize_y>", appended): here
+ * "<GPU name> | <sx> | 32 | <tile rows> | <stages> | <form>".  The
+ * reference's loader reads these lines as 32 x rows blocks; lines without
+ * the last two fields are not ours and are skipped.
+ * FLETCHER_Autotune(path, steps_per_shape), after DRIVER_Initialize: when
+ * path holds a line for this GPU, sx and storage form, that shape is applied
+ * at once (returns 1).  Otherwise (returns 0) the next steps, through any
+ * entry point, try each built shape for 1 + steps_per_shape steps -- the
+ * simulation advances normally; results do not depend on the shape -- and
+ * the fastest is then applied and appended to path.
+ * FLETCHER_GetTileConfig: the current shape; returns 1 while tuning. */
+int FLETCHER_Autotune(const char *path, int steps_per_shape);
+int FLETCHER_GetTileConfig(int *tile_rows, int *stages);
+int FLETCHER_TuneConfigLookup(const char *path, const char *gpu_name, int sx, int form, int *tile_rows,
+                              int *stages);
+int FLETCHER_TuneConfigStore(const char *path, const char *gpu_name, int sx, int form, int tile_rows, int stages);
+
 /* Runs nsteps steps back to back on the stream without host
  * synchronisation: step s adds src[s] at iSource (iSource < 0: no source),
  * then propagates.  Equivalent to nsteps x (DRIVER_InsertSource +
