@@ -43,6 +43,8 @@ def load():
         lib.orc_propagate_f32.argtypes = [C.c_int] * 4 + [C.c_float] * 4 + [FP] * 5
         lib.orc_run_f32.argtypes = [C.c_int] * 4 + [C.c_float] * 4 + [C.c_int, C.c_long, C.c_double] + [FP] * 5
         lib.orc_run_f32.restype = C.c_int
+        lib.orc_run_d1d1_f32.argtypes = lib.orc_run_f32.argtypes
+        lib.orc_run_d1d1_f32.restype = C.c_int
         lib.orc_run_f64.argtypes = [C.c_int] * 4 + [C.c_double] * 4 + [C.c_int, C.c_long, C.c_double] + [DP] * 5
         lib.orc_run_f64.restype = C.c_int
         lib.orc_threads.restype = C.c_int
@@ -105,6 +107,19 @@ def run_f32(prob, model: np.ndarray, steps: int | None = None, coef: np.ndarray 
         pp, pc, qp, qc = (np.array(f, np.float32, copy=True).reshape(n) for f in fields)
     odd = lib.orc_run_f32(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, st,
                           prob.i_source, prob.fcut, _fp(pp), _fp(pc), _fp(qp), _fp(qc), _fp(coef))
+    return (pp, qp, pc, qc) if odd else (pc, qc, pp, qp)
+
+
+def run_d1d1_f32(prob, model: np.ndarray, steps: int | None = None):
+    """FP32 oracle run of the Der1-Der1 formulation (der1der1/ tree);
+    returns (p, q, pp, qp) final current/previous fields."""
+    lib = load()
+    st = prob.steps if steps is None else steps
+    coef = precompute(model)
+    n = prob.n
+    pp, pc, qp, qc = (np.zeros(n, np.float32) for _ in range(4))
+    odd = lib.orc_run_d1d1_f32(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, st,
+                               prob.i_source, prob.fcut, _fp(pp), _fp(pc), _fp(qp), _fp(qc), _fp(coef))
     return (pp, qp, pc, qc) if odd else (pc, qc, pp, qp)
 
 

@@ -351,6 +351,118 @@ int orc_run_f32(int sx, int sy, int sz, int bord, float dx, float dy, float dz, 
   return st & 1;
 }
 
+/* Der1 of the Der1-Der1 tree, der1der1/derivatives.h:45: 9-point first
+ * derivative, summed in the macro's order and scaled last. */
+static inline float der1_f(const float *p, long i, long s, float dinv) {
+  return ((L1f * (p[i + s] - p[i - s]) + L2f * (p[i + 2 * s] - p[i - 2 * s]) +
+           L3f * (p[i + 3 * s] - p[i - 3 * s]) + L4f * (p[i + 4 * s] - p[i - 4 * s])) *
+          (dinv));
+}
+
+/*
+ * One FP32 step of the Der1-Der1 formulation: der1der1/OpenMP/openmp_propagate.c:9-100
+ * with der1der1/sample.h.  First derivatives of p and q are stored
+ * (pDx, qDx over x in [bord, sx-bord) for every y and z; pDy, qDy over
+ * y in [bord, sy-bord) and x in [bord, sx)), and the mixed derivatives are
+ * first derivatives of them: pxy = Der1_y(pDx), pxz = Der1_z(pDx),
+ * pyz = Der1_z(pDy).  The rest is the update of original/sample.h:32-89.
+ * `work` holds 4 * sx*sy*sz floats (pDx, pDy, qDx, qDy).
+ */
+void orc_propagate_d1d1_f32(int sx, int sy, int sz, int bord, float dx, float dy, float dz, float dt,
+                            float *restrict pp, const float *restrict pc, float *restrict qp,
+                            const float *restrict qc, const float *restrict coef, float *restrict work) {
+  const long n = (long)sx * sy * sz;
+  const float *ch1dxx = coef + C_XX * n, *ch1dyy = coef + C_YY * n, *ch1dzz = coef + C_ZZ * n;
+  const float *ch1dxy = coef + C_XY * n, *ch1dyz = coef + C_YZ * n, *ch1dxz = coef + C_XZ * n;
+  const float *v2px = coef + C_V2PX * n, *v2pz = coef + C_V2PZ * n, *v2sz = coef + C_V2SZ * n;
+  const float *v2pn = coef + C_V2PN * n;
+  float *pDx = work, *pDy = work + n, *qDx = work + 2 * n, *qDy = work + 3 * n;
+  const long strideX = 1, strideY = sx, strideZ = (long)sx * sy;
+  const float dxxinv = 1.0f / (dx * dx);
+  const float dyyinv = 1.0f / (dy * dy);
+  const float dzzinv = 1.0f / (dz * dz);
+  const float dxinv = 1.0f / dx;
+  const float dyinv = 1.0f / dy;
+  const float dzinv = 1.0f / dz;
+#pragma omp parallel
+  {
+#pragma omp for nowait
+    for (int iz = 0; iz < sz; iz++)
+      for (int iy = 0; iy < sy; iy++)
+        for (long i = ORC_IND(bord, iy, iz); i < ORC_IND(sx - bord, iy, iz); i++) pDx[i] = der1_f(pc, i, strideX, dxinv);
+#pragma omp for nowait
+    for (int iz = 0; iz < sz; iz++)
+      for (int iy = bord; iy < sy - bord; iy++)
+        for (long i = ORC_IND(bord, iy, iz); i < ORC_IND(sx, iy, iz); i++) pDy[i] = der1_f(pc, i, strideY, dyinv);
+#pragma omp for nowait
+    for (int iz = 0; iz < sz; iz++)
+      for (int iy = 0; iy < sy; iy++)
+        for (long i = ORC_IND(bord, iy, iz); i < ORC_IND(sx - bord, iy, iz); i++) qDx[i] = der1_f(qc, i, strideX, dxinv);
+#pragma omp for
+    for (int iz = 0; iz < sz; iz++)
+      for (int iy = bord; iy < sy - bord; iy++)
+        for (long i = ORC_IND(bord, iy, iz); i < ORC_IND(sx, iy, iz); i++) qDy[i] = der1_f(qc, i, strideY, dyinv);
+#pragma omp for
+    for (int iz = bord; iz < sz - bord; iz++)
+      for (int iy = bord; iy < sy - bord; iy++)
+        for (int ix = bord; ix < sx - bord; ix++) {
+          const long i = ORC_IND(ix, iy, iz);
+          const float pxy = der1_f(pDx, i, strideY, dyinv);
+          const float pxz = der1_f(pDx, i, strideZ, dzinv);
+          const float pyz = der1_f(pDy, i, strideZ, dzinv);
+          const float pxx = der2_f(pc, i, strideX, dxxinv);
+          const float pyy = der2_f(pc, i, strideY, dyyinv);
+          const float pzz = der2_f(pc, i, strideZ, dzzinv);
+          const float cpxx = ch1dxx[i] * pxx;
+          const float cpyy = ch1dyy[i] * pyy;
+          const float cpzz = ch1dzz[i] * pzz;
+          const float cpxy = ch1dxy[i] * pxy;
+          const float cpxz = ch1dxz[i] * pxz;
+          const float cpyz = ch1dyz[i] * pyz;
+          const float h1p = cpxx + cpyy + cpzz + cpxy + cpxz + cpyz;
+          const float h2p = pxx + pyy + pzz - h1p;
+          const float qxy = der1_f(qDx, i, strideY, dyinv);
+          const float qxz = der1_f(qDx, i, strideZ, dzinv);
+          const float qyz = der1_f(qDy, i, strideZ, dzinv);
+          const float qxx = der2_f(qc, i, strideX, dxxinv);
+          const float qyy = der2_f(qc, i, strideY, dyyinv);
+          const float qzz = der2_f(qc, i, strideZ, dzzinv);
+          const float cqxx = ch1dxx[i] * qxx;
+          const float cqyy = ch1dyy[i] * qyy;
+          const float cqzz = ch1dzz[i] * qzz;
+          const float cqxy = ch1dxy[i] * qxy;
+          const float cqxz = ch1dxz[i] * qxz;
+          const float cqyz = ch1dyz[i] * qyz;
+          const float h1q = cqxx + cqyy + cqzz + cqxy + cqxz + cqyz;
+          const float h2q = qxx + qyy + qzz - h1q;
+          const float h1pmq = h1p - h1q;
+          const float h2pmq = h2p - h2q;
+          const float rhsp = v2px[i] * h2p + v2pz[i] * h1q + v2sz[i] * h1pmq;
+          const float rhsq = v2pn[i] * h2p + v2pz[i] * h1q - v2sz[i] * h2pmq;
+          pp[i] = 2.0f * pc[i] - pp[i] + rhsp * dt * dt;
+          qp[i] = 2.0f * qc[i] - qp[i] + rhsq * dt * dt;
+        }
+  }
+}
+
+/* The time loop of orc_run_f32 with the Der1-Der1 step. */
+int orc_run_d1d1_f32(int sx, int sy, int sz, int bord, float dx, float dy, float dz, float dt, int st,
+                     long iSource, double fcut, float *pp, float *pc, float *qp, float *qc, const float *coef) {
+  const long n = (long)sx * sy * sz;
+  float *work = (float *)calloc((size_t)(4 * n), sizeof(float));
+  if (!work) return -1;
+  for (int it = 1; it <= st; it++) {
+    float src = orc_source(dt, it - 1, fcut);
+    pc[iSource] += src;
+    qc[iSource] += src;
+    orc_propagate_d1d1_f32(sx, sy, sz, bord, dx, dy, dz, dt, pp, pc, qp, qc, coef, work);
+    float *t = pp; pp = pc; pc = t;
+    t = qp; qp = qc; qc = t;
+  }
+  free(work);
+  return st & 1;
+}
+
 /* FP64 time loop: same sequence, double fields, double source values. */
 int orc_run_f64(int sx, int sy, int sz, int bord, double dx, double dy, double dz, double dt,
                 int st, long iSource, double fcut, double *pp, double *pc, double *qp, double *qc,

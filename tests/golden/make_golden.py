@@ -9,6 +9,7 @@ the reference's RandomVelocityBoundary applied inside the reference build.
     python tests/golden/make_golden.py            # small cases (minutes)
     python tests/golden/make_golden.py --c1       # + the 504^3, 1000-step case (about an hour)
     python tests/golden/make_golden.py --c2-f64   # FP64 oracle, 128^3 interior, 2000 steps (minutes)
+    python tests/golden/make_golden.py --d1d1     # the der1der1/ tree (Der1-Der1 formulation), small cases
 
 Each fixture stores the problem definition, hashes of the boundary-modified
 velocities and of the reference's coefficient fields, and the final current
@@ -43,9 +44,12 @@ def sha(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-def ref_lib():
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
-    lib = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libfletcher_ref.so"))
+def ref_lib(tree: str = "original"):
+    """The harness over the reference's OpenMP back-end of `tree` ("original"
+    or "der1der1", the Der1-Der1 formulation)."""
+    target, name = ("ref", "libfletcher_ref.so") if tree == "original" else ("ref_d1d1", "libfletcher_ref_d1d1.so")
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), target], check=True)
+    lib = C.CDLL(os.path.join(ROOT, "oracle", "_ref", name))
     lib.ref_boundary.argtypes = [C.c_int] * 8 + [FP, FP, C.c_uint]
     lib.ref_precompute.argtypes = [C.c_int] * 4 + [FP] * 7
     lib.ref_run.argtypes = [C.c_int] * 4 + [C.c_float] * 4 + [C.c_int, C.c_int, C.c_double] + [FP] * 10
@@ -179,9 +183,18 @@ def main() -> None:
     ap.add_argument("--c1", action="store_true", help="also run the 504^3 x 1000-step case")
     ap.add_argument("--only-c1", action="store_true")
     ap.add_argument("--c2-f64", action="store_true", help="only the FP64 oracle's 128^3, 2000-step case")
+    ap.add_argument("--d1d1", action="store_true", help="only the Der1-Der1 tree's small cases")
     a = ap.parse_args()
     if a.c2_f64:
         run_c2_f64()
+        return
+    if a.d1d1:
+        lib = ref_lib("der1der1")
+        lay = Problem("d1d1_layered", 24, 20, 16, absorb=6, dt=0.0006, steps=60, fcut=45.0, kind="layered",
+                      layers=4, seed=3)
+        lay = lay.with_(source=(lay.sx // 2 + 3, lay.sy // 2 - 2, lay.bord + lay.absorb + 4))
+        run_small(lib, "d1d1_tiny_layered", lay)
+        run_small(lib, "d1d1_c0", C0, stride=3)
         return
     if not a.only_c1:
         lib = ref_lib()

@@ -240,3 +240,21 @@ def test_c1_full_size_vs_reference():
     es = rel_l2(np.sqrt(plane_sums(p, prob)), np.sqrt(g["psum"]))
     print(f"C1 504^3 x 1000 steps vs reference: rel L2 p {ep:.3e} q {eq:.3e} plane energy {es:.3e}")
     assert ep < TOL_C1 and eq < TOL_C1 and es < TOL_C1
+
+
+@pytest.mark.parametrize("name", ["d1d1_tiny_layered", "d1d1_c0"])
+def test_vs_der1der1_reference(name, orc):
+    """The GPU path against the der1der1/ tree's output (the Der1-Der1
+    formulation): the same 1e-5 bound as against original/.  The GPU's
+    mixed derivatives are first derivatives of first derivatives too, so it
+    is closer to this tree than to original/'s 64-point sums."""
+    prob, meta, g = load_golden(name)
+    m = prob.model()
+    p, q, _, _ = gpu_run(prob, m)
+    s = meta["stride"]
+    e_d1d1 = rel_l2(subsample(p, prob, s), g["p"])
+    op, _, _, _ = orc.run_f32(prob, m)
+    e_orig = rel_l2(subsample(p, prob, s), subsample(op, prob, s))
+    print(f"{name}: GPU vs der1der1 {e_d1d1:.3g}, vs original {e_orig:.3g}")
+    assert e_d1d1 < TOL_SHORT
+    assert rel_l2(subsample(q, prob, s), g["q"]) < TOL_SHORT

@@ -78,3 +78,21 @@ def test_fp64_oracle_close_to_fp32(orc):
     p64, q64 = orc.run_f64(prob, m)
     assert orc.rel_l2(g["p"], p64) < 1e-5
     assert orc.rel_l2(g["q"], q64) < 1e-5
+
+
+@pytest.mark.parametrize("name", ["d1d1_tiny_layered", "d1d1_c0"])
+def test_der1der1_restatement_bit_identical(name, orc):
+    """The Der1-Der1 restatement (orc_propagate_d1d1_f32) against the
+    der1der1/ tree's own OpenMP build: identical floats."""
+    prob, meta, g = load_golden(name)
+    m = orc.boundary(prob.sx, prob.sy, prob.sz, prob.nx, prob.ny, prob.nz, prob.bord, prob.absorb,
+                     prob.raw_model(), prob.seed)
+    assert sha(m[0]) == meta["vpz_sha"]
+    p, q, _, _ = orc.run_d1d1_f32(prob, m)
+    s = meta["stride"]
+    assert np.array_equal(subsample(p, prob, s), g["p"])
+    assert np.array_equal(subsample(q, prob, s), g["q"])
+    # the two formulations differ by rounding only
+    op, oq, _, _ = orc.run_f32(prob, m)
+    d = np.linalg.norm(p.astype(np.float64) - op) / np.linalg.norm(op)
+    assert 0.0 < d < 1e-5
