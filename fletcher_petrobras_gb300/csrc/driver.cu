@@ -54,6 +54,7 @@ struct State {
   long launches = 0;
   size_t dev_bytes = 0;
   int num_sms = 0;
+  bool hostmem = false;  // kernels read and write the caller's host arrays directly
   int form = FLETCHER_FORM_FP32;
   unsigned *Hh[2] = {nullptr, nullptr};
   unsigned short *Hl[2] = {nullptr, nullptr};
@@ -83,6 +84,7 @@ bool g_own_stream = false;
 int g_form = FLETCHER_FORM_FP32;
 int g_req_rows = 0, g_req_stages = 0, g_req_chunks = 0;
 int g_errmode = FLETCHER_ERRMODE_EXIT;
+int g_host_access = -1;  // -1: use direct host access where the device supports it; 0: never
 int g_last_err = FLETCHER_OK;
 char g_errmsg[512] = "";
 
@@ -132,20 +134,28 @@ namespace {
 
 // ---- auxiliary kernels --------------------------------------------------------
 
+// The six raw model arrays (vpz vsv epsilon delta phi theta): device copies,
+// or the caller's host arrays where the GPU reads host memory directly.
+struct Raw6 {
+  const float *a[6];
+};
+
 // Coefficient precompute, original/precomp.h:14-38 and :49-58: trigonometry
 // in FP64 rounded to float, products of those floats in float, velocity
-// terms in FP64.  raw = vpz vsv epsilon delta phi theta (n floats each).
-__global__ void k_precompute(const float *__restrict__ raw, float *__restrict__ coef, int sx, int sy, int sz,
-                             int pitch) {
+// terms in FP64.
+__global__ void k_precompute(Raw6 raw, float *__restrict__ coef, int sx, int sy, int sz, int pitch) {
   const size_t n = (size_t)sx * sy * sz;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const float vpz = raw[i], vsv = raw[n + i], eps = raw[2 * n + i], del = raw[3 * n + i];
-    const float phi = raw[4 * n + i], theta = raw[5 * n + i];
-    const float sinTheta = (float)sin((double)theta);
-    const float cosTheta = (float)cos((double)theta);
+    const float vpz = raw.a[0][i], vsv = raw.a[1][i], eps = raw.a[2][i], del = raw.a[3][i];
+    const float phi = raw.a[4][i], theta = raw.a[5][i];
+    double st, ct, sp, cp;
+    sincos((double)theta, &st, &ct);
+    sincos((double)phi, &sp, &cp);
+    const float sinTheta = (float)st;
+    const float cosTheta = (float)ct;
     const float sin2Theta = (float)sin(__dmul_rn(2.0, (double)theta));
-    const float sinPhi = (float)sin((double)phi);
-    const float cosPhi = (float)cos((double)phi);
+    const float sinPhi = (float)sp;
+    const float cosPhi = (float)cp;
     const float sin2Phi = (float)sin(__dmul_rn(2.0, (double)phi));
     const float v2sz = __fmul_rn(vsv, vsv);
     const float v2pz = __fmul_rn(vpz, vpz);
@@ -495,13 +505,25 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   g.dev_bytes += g.npitch * kNumCoef * sizeof(float) + g.n * sizeof(float);
   CK(cudaMemsetAsync(g.coef, 0, g.npitch * kNumCoef * sizeof(float), s));
 
-  // Raw model arrays -> coefficients (temporary 6-volume buffer).
+  // Raw model arrays -> coefficients.  On systems whose GPU reads pageable
+  // host memory (Grace over NVLink-C2C) the kernels read the caller's arrays
+  // in place; elsewhere they go through a temporary 6-volume device buffer.
+  int pma = 0;
+  CK(cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev));
+  g.hostmem = pma && g_host_access != 0;
   float *raw = nullptr;
-  CK(cudaMalloc(&raw, 6 * g.n * sizeof(float)));
   const float *src6[6] = {vpz, vsv, epsilon, delta, phi, theta};
-  for (int k = 0; k < 6; ++k)
-    CK(cudaMemcpyAsync(raw + k * g.n, src6[k], g.n * sizeof(float), cudaMemcpyHostToDevice, s));
-  k_precompute<<<grid_for(g.n), 256, 0, s>>>(raw, g.coef, sx, sy, sz, g.pitch);
+  Raw6 r6;
+  if (g.hostmem) {
+    for (int k = 0; k < 6; ++k) r6.a[k] = src6[k];
+  } else {
+    CK(cudaMalloc(&raw, 6 * g.n * sizeof(float)));
+    for (int k = 0; k < 6; ++k) {
+      CK(cudaMemcpyAsync(raw + k * g.n, src6[k], g.n * sizeof(float), cudaMemcpyHostToDevice, s));
+      r6.a[k] = raw + k * g.n;
+    }
+  }
+  k_precompute<<<grid_for(g.n), 256, 0, s>>>(r6, g.coef, sx, sy, sz, g.pitch);
   CK(cudaGetLastError());
   // Initial fields (the reference's OpenMP back-end works on the caller's
   // arrays, so their contents are the initial state).
@@ -510,20 +532,25 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   const float *fp[2][2] = {{pc, qc}, {pp, qp}};
   for (int b = 0; b < 2; ++b) {
     const float *p = fp[b][0], *q = fp[b][1];
-    if (p) CK(cudaMemcpyAsync(raw, p, g.n * sizeof(float), cudaMemcpyHostToDevice, s));
-    if (q) CK(cudaMemcpyAsync(raw + g.n, q, g.n * sizeof(float), cudaMemcpyHostToDevice, s));
+    if (!g.hostmem) {
+      // The coefficient kernel has finished with `raw` before these copies
+      // (same stream).
+      if (p) CK(cudaMemcpyAsync(raw, p, g.n * sizeof(float), cudaMemcpyHostToDevice, s));
+      if (q) CK(cudaMemcpyAsync(raw + g.n, q, g.n * sizeof(float), cudaMemcpyHostToDevice, s));
+      p = p ? raw : nullptr;
+      q = q ? raw + g.n : nullptr;
+    }
     if (half) {
       // Buffer 0 holds the current field (exponent slot 0), buffer 1 the
       // previous one (slot 2).
-      CK(half_encode(p ? raw : nullptr, q ? raw + g.n : nullptr, g.Hh[b], g.Hl[b], g.E + (b ? 2 : 0) * sz,
-                     g.Mx + b * sz, sx, sy, sz, g.pitch, ext, s));
+      CK(half_encode(p, q, g.Hh[b], g.Hl[b], g.E + (b ? 2 : 0) * sz, g.Mx + b * sz, sx, sy, sz, g.pitch, ext, s));
     } else {
-      k_pack<<<grid_for(g.n), 256, 0, s>>>(p ? raw : nullptr, q ? raw + g.n : nullptr, g.F[b], sx, sy, sz, g.pitch);
+      k_pack<<<grid_for(g.n), 256, 0, s>>>(p, q, g.F[b], sx, sy, sz, g.pitch);
       CK(cudaGetLastError());
     }
   }
   CK(cudaStreamSynchronize(s));
-  CK(cudaFree(raw));
+  if (raw) CK(cudaFree(raw));
 
   if (setup_tiles(rows, stages)) return g_last_err;
   g.launches = 0;
@@ -664,15 +691,18 @@ int step() {
 // Component comp of buffer buf (which holds the current field when buf ==
 // g.cur) -> host.
 int read_component(int buf, int comp, float *host) {
+  // Where the GPU writes host memory directly, the kernel writes the
+  // caller's array; otherwise it goes through `scratch` and a copy.
+  float *out = g.hostmem ? host : g.scratch;
   if (half_form()) {
     const int slot = buf == g.cur ? g.ecur : (g.ecur + 2) % 3;
-    CK(half_decode(g.Hh[buf], g.Hl[buf], g.E + slot * g.sz, g.scratch, comp, g.sx, g.sy, g.sz, g.pitch,
+    CK(half_decode(g.Hh[buf], g.Hl[buf], g.E + slot * g.sz, out, comp, g.sx, g.sy, g.sz, g.pitch,
                    g.form == FLETCHER_FORM_FP16X, grid_for(g.n), g_stream));
   } else {
-    k_unpack<<<grid_for(g.n), 256, 0, g_stream>>>(g.F[buf], g.scratch, comp, g.sx, g.sy, g.sz, g.pitch);
+    k_unpack<<<grid_for(g.n), 256, 0, g_stream>>>(g.F[buf], out, comp, g.sx, g.sy, g.sz, g.pitch);
     CK(cudaGetLastError());
   }
-  CK(cudaMemcpyAsync(host, g.scratch, g.n * sizeof(float), cudaMemcpyDeviceToHost, g_stream));
+  if (!g.hostmem) CK(cudaMemcpyAsync(host, g.scratch, g.n * sizeof(float), cudaMemcpyDeviceToHost, g_stream));
   CK(cudaStreamSynchronize(g_stream));
   return check_err_word();
 }
@@ -801,6 +831,14 @@ extern "C" int FLETCHER_SetStream(void *s) {
   return FLETCHER_OK;
 }
 extern "C" void *FLETCHER_GetStream(void) { return g_stream; }
+
+extern "C" int FLETCHER_SetHostAccess(int mode) {
+  if (mode != -1 && mode != 0) return fail(FLETCHER_ERR_ARGS, "FLETCHER_SetHostAccess: mode must be -1 or 0");
+  g_host_access = mode;
+  return FLETCHER_OK;
+}
+
+extern "C" int FLETCHER_HostAccess(void) { return g.init && g.hostmem ? 1 : 0; }
 
 extern "C" int FLETCHER_SetForm(int form) {
   if (form < FLETCHER_FORM_FP32 || form > FLETCHER_FORM_FP16X)
@@ -1172,7 +1210,9 @@ extern "C" int FLETCHER_BatchAddShot(int sx, int sy, int sz, const float *model,
   cudaError_t e = cudaMemcpyAsync(raw, model, 6 * s.n * sizeof(float), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(s.coef, 0, s.npitch * kNumCoef * sizeof(float), st);
   if (e == cudaSuccess) {
-    k_precompute<<<grid_for(s.n), 256, 0, st>>>(raw, s.coef, sx, sy, sz, s.pitch);
+    Raw6 r6;
+    for (int k = 0; k < 6; ++k) r6.a[k] = raw + k * s.n;
+    k_precompute<<<grid_for(s.n), 256, 0, st>>>(r6, s.coef, sx, sy, sz, s.pitch);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemsetAsync(s.F[0], 0, s.npitch * sizeof(float2), st);

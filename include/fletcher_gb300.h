@@ -80,6 +80,16 @@ void FLETCHER_ClearError(void);
 int FLETCHER_SetStream(void *cuda_stream);
 void *FLETCHER_GetStream(void);
 
+/* Host arrays.  Where the GPU reads and writes pageable host memory itself
+ * (cudaDevAttrPageableMemoryAccess, e.g. Grace over NVLink-C2C),
+ * DRIVER_Initialize's kernels read the caller's model and field arrays in
+ * place and read-backs write the caller's arrays directly; elsewhere both
+ * go through device buffers and copies.  FLETCHER_SetHostAccess(0), before
+ * DRIVER_Initialize, forces the copies (-1: automatic, the default);
+ * FLETCHER_HostAccess() tells which path the resident state uses. */
+int FLETCHER_SetHostAccess(int mode);
+int FLETCHER_HostAccess(void);
+
 /* Storage form of the wave fields, chosen before DRIVER_Initialize.
  * FLETCHER_FORM_FP32: p,q in FP32 (the reference's precision).
  * FLETCHER_FORM_FP16: p,q stored as FP16 with one power-of-two scale per

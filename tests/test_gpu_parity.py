@@ -258,3 +258,28 @@ def test_vs_der1der1_reference(name, orc):
     print(f"{name}: GPU vs der1der1 {e_d1d1:.3g}, vs original {e_orig:.3g}")
     assert e_d1d1 < TOL_SHORT
     assert rel_l2(subsample(q, prob, s), g["q"]) < TOL_SHORT
+
+
+def test_host_access_and_copy_paths_identical():
+    """DRIVER_Initialize and the read-backs through the GPU's direct access
+    to the caller's host arrays (where the device has it) and through
+    device buffers and copies give identical coefficients and fields."""
+    prob = Problem("hostmem", 30, 28, 26, absorb=4, dt=0.0006, steps=12, fcut=45.0, kind="layered", layers=3, seed=2)
+    m = prob.model()
+    g = np.random.default_rng(4)
+    init = [(1e-3 * g.standard_normal(prob.n)).astype(np.float32) for _ in range(4)]
+    out, modes = [], []
+    for mode in (-1, 0):
+        prop = Propagator()
+        prop.lib.FLETCHER_SetHostAccess(mode)
+        prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, m, *init)
+        modes.append(prop.lib.FLETCHER_HostAccess())
+        prop.run(prob.steps, prob.i_source, prob.sources())
+        prop.synchronize()
+        out.append([prop.field(k) for k in range(4)] + [prop.coefficients()])
+        prop.finalize()
+        prop.lib.FLETCHER_SetHostAccess(-1)
+    print("direct host access:", modes)
+    assert modes[1] == 0
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
