@@ -80,12 +80,12 @@ void FLETCHER_ClearError(void);
 int FLETCHER_SetStream(void *cuda_stream);
 void *FLETCHER_GetStream(void);
 
-/* Host arrays.  Where the GPU reads and writes pageable host memory itself
- * (cudaDevAttrPageableMemoryAccess, e.g. Grace over NVLink-C2C),
- * DRIVER_Initialize's kernels read the caller's model and field arrays in
- * place and read-backs write the caller's arrays directly; elsewhere both
- * go through device buffers and copies.  FLETCHER_SetHostAccess(0), before
- * DRIVER_Initialize, forces the copies (-1: automatic, the default);
+/* Host arrays.  By default DRIVER_Initialize copies the caller's model and
+ * field arrays to device buffers, and read-backs copy to the caller's
+ * arrays.  FLETCHER_SetHostAccess(1), before DRIVER_Initialize, lets the
+ * kernels read and write the caller's arrays in place where the GPU
+ * accesses pageable host memory (cudaDevAttrPageableMemoryAccess, e.g.
+ * Grace over NVLink-C2C); on GB300 that measured slower than the copies.
  * FLETCHER_HostAccess() tells which path the resident state uses. */
 int FLETCHER_SetHostAccess(int mode);
 int FLETCHER_HostAccess(void);
