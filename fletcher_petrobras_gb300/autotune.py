@@ -11,7 +11,7 @@ from __future__ import annotations
 import json
 import os
 
-CANDIDATES = [(12, 5), (12, 4), (12, 6), (16, 5), (8, 5)]
+CANDIDATES = [(16, 5), (16, 4), (12, 5), (12, 4), (12, 6), (8, 5)]
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 
 

@@ -441,7 +441,9 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
     return fail(FLETCHER_ERR_ARGS, "unknown storage form %d", g_form);
   const bool half = g_form != FLETCHER_FORM_FP32;
   const bool ext = g_form == FLETCHER_FORM_FP16X;
-  const int rows = g_req_rows ? g_req_rows : 12;
+  // Default shapes (measured at 504^3): FP32 16 rows x 5 stages (2.20 ms per
+  // step against 2.40 for 12 x 5); the 16-bit forms 12 x 5.
+  const int rows = g_req_rows ? g_req_rows : (half ? 12 : 16);
   const int stages = g_req_stages ? g_req_stages : 5;
   if (!(half ? propagate_half_supported(rows, stages) : propagate_fp32_supported(rows, stages)))
     return fail(FLETCHER_ERR_ARGS, "tile shape (%d rows, %d stages) is not built for form %d", rows, stages, g_form);
@@ -851,7 +853,7 @@ extern "C" int FLETCHER_SetForm(int form) {
 }
 
 extern "C" int FLETCHER_SetTileConfig(int rows, int stages, int zchunks) {
-  const int r = rows ? rows : 12, s = stages ? stages : 5;
+  const int r = rows ? rows : 16, s = stages ? stages : 5;
   if (!propagate_fp32_supported(r, s) && !propagate_half_supported(r, s))
     return fail(FLETCHER_ERR_ARGS, "tile shape (%d, %d) is not built", r, s);
   if (zchunks < 0) return fail(FLETCHER_ERR_ARGS, "zchunks must be >= 0");
@@ -1175,7 +1177,7 @@ extern "C" int FLETCHER_BatchCreate(int bord, float dx, float dy, float dz, floa
   B.open = true;
   B.bord = bord;
   B.dx = dx; B.dy = dy; B.dz = dz; B.dt = dt;
-  B.rows = g_req_rows ? g_req_rows : 12;
+  B.rows = g_req_rows ? g_req_rows : 16;
   B.stages = g_req_stages ? g_req_stages : 5;
   return FLETCHER_OK;
 }
@@ -1313,7 +1315,7 @@ extern "C" int FLETCHER_BatchGetField(int shot, int which, float *host) {
 
 extern "C" int FLETCHER_BatchSetTileConfig(int rows, int stages) {
   if (!B.open) return fail(FLETCHER_ERR_ARGS, "no batch");
-  const int r = rows ? rows : 12, s = stages ? stages : 5;
+  const int r = rows ? rows : 16, s = stages ? stages : 5;
   if (!propagate_fp32_supported(r, s)) return fail(FLETCHER_ERR_ARGS, "tile shape (%d, %d) is not built", r, s);
   B.rows = r;
   B.stages = s;

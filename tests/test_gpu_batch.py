@@ -72,7 +72,7 @@ def test_batch_tile_shapes_and_rerun_identical():
     batch.run()
     a = [batch.field(i, 0) for i in range(len(SHOTS))]
     batch.reset()
-    batch.set_tile(16, 5)
+    batch.set_tile(12, 5)  # the default is 16 x 5
     batch.run()
     b = [batch.field(i, 0) for i in range(len(SHOTS))]
     batch.close()
