@@ -49,10 +49,10 @@ struct Geo {
   static constexpr int OFF_PP = OFF_UPD + UPD_B;
   static constexpr int STAGE_B = (OFF_PP + PP_B + 127) / 128 * 128;
   static constexpr int DBUF_B = 2 * TY * HX * 8;  // D1y rows with their x halo, double-buffered
-  // Tiles of 16 rows (512 threads, at most 128 registers a thread) keep the
-  // per-cell in-plane terms (A, B) of the last 5 planes in shared memory
-  // instead of a 9-plane register ring.
-  static constexpr bool AB_SMEM = TY >= 16;
+  // Tiles of 16 rows (512 threads, at most 128 registers a thread), and of 8
+  // rows (two CTAs per SM), keep the per-cell in-plane terms (A, B) of the
+  // last 5 planes in shared memory instead of a 9-plane register ring.
+  static constexpr bool AB_SMEM = TY >= 16 || TY <= 8;  // 8 rows run two CTAs per SM (128 registers)
   static constexpr int AB_B = AB_SMEM ? 5 * NT * 16 : 0;
   static_assert(TY % 4 == 0, "tile rows must be a multiple of 4");
   static_assert(HALO_B % 128 == 0 && ARR_B % 128 == 0 && UPD_B % 128 == 0, "stage regions 128-B aligned");
@@ -445,7 +445,7 @@ static cudaError_t launch_t(const PropLaunch &L, cudaStream_t s) {
 
 // Supported shapes: rows per tile x stages.  TY = 16 runs one 512-thread CTA
 // per SM; TY = 8 runs two 256-thread CTAs per SM.
-#define FLT_SHAPES(X) X(12, 4, 1) X(12, 5, 1) X(12, 6, 1) X(16, 4, 1) X(16, 5, 1) X(8, 5, 2)
+#define FLT_SHAPES(X) X(12, 4, 1) X(12, 5, 1) X(12, 6, 1) X(16, 4, 1) X(16, 5, 1) X(8, 4, 2) X(8, 5, 2)
 
 size_t propagate_fp32_smem_bytes(int ty, int st) {
 #define X(a, b, c) \
