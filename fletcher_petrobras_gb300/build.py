@@ -21,7 +21,7 @@ EXE = os.path.join(OUT, "fletcher_gb300")
 
 NVCC = os.environ.get("NVCC", "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = GENCODE + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-fopenmp",
+NVCC_FLAGS = GENCODE + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                         "-Xptxas", "-v", "-I" + INCLUDE]
 CC = os.environ.get("CC", "gcc")
 C_FLAGS = ["-O3", "-fPIC", "-ffp-contract=off", "-std=gnu11", "-Wall", "-I" + INCLUDE]
@@ -71,7 +71,7 @@ def build(verbose: bool = False) -> str:
             for f in [ex.submit(_run, c, l) for c, l in jobs]:
                 f.result()
     if jobs or _newer(LIB, objs):
-        _run([NVCC] + GENCODE + ["-shared", "-o", LIB] + objs + ["-lm", "-lgomp"])
+        _run([NVCC] + GENCODE + ["-shared", "-o", LIB] + objs + ["-lm"])
     main_c = os.path.join(CSRC, "host", "fletcher_main.c")
     if _newer(EXE, [main_c, LIB]):
         _run([CC] + C_FLAGS + ["-o", EXE, main_c, "-L" + OUT, "-lfletcher_gb300",

@@ -19,8 +19,6 @@
 #include <stdlib.h>
 #include <string.h>
 
-#include <omp.h>
-
 #include <vector>
 
 #include "../../include/fletcher_gb300.h"
@@ -222,91 +220,6 @@ __global__ void k_add_source(float2 *F, size_t idx, float val) {
     v.y = v.y + val;
     F[idx] = v;
   }
-}
-
-// ---- host <-> device transfers of the caller's (pageable) arrays ---------------
-//
-// Large transfers go through two page-locked staging buffers: host threads
-// copy one chunk into a buffer while the copy engine moves the other one,
-// which is several times faster than the runtime's single-threaded staging
-// of pageable memory.
-
-constexpr size_t kStageChunk = size_t(128) << 20;
-
-struct Staging {
-  void *buf[2] = {nullptr, nullptr};
-  cudaEvent_t ev[2] = {nullptr, nullptr};
-};
-Staging g_stage;
-
-void par_memcpy(void *dst, const void *src, size_t bytes) {
-  const size_t per = size_t(4) << 20;
-  const long nb = (long)((bytes + per - 1) / per);
-#pragma omp parallel for schedule(static) if (nb > 1)
-  for (long b = 0; b < nb; ++b) {
-    const size_t o = (size_t)b * per, n = bytes - o < per ? bytes - o : per;
-    memcpy(static_cast<char *>(dst) + o, static_cast<const char *>(src) + o, n);
-  }
-}
-
-cudaError_t ensure_staging() {
-  if (g_stage.buf[0]) return cudaSuccess;
-  for (int k = 0; k < 2; ++k) {
-    cudaError_t e = cudaHostAlloc(&g_stage.buf[k], kStageChunk, cudaHostAllocDefault);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g_stage.ev[k], cudaEventDisableTiming);
-    if (e != cudaSuccess) return e;
-  }
-  return cudaSuccess;
-}
-
-// host -> device, ordered on stream s; returns when the host array may be reused.
-cudaError_t upload(void *dev, const void *host, size_t bytes, cudaStream_t s) {
-  if (bytes < (size_t(32) << 20)) return cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, s);
-  cudaError_t e = ensure_staging();
-  if (e != cudaSuccess) return e;
-  for (size_t off = 0, i = 0; off < bytes; off += kStageChunk, ++i) {
-    const int k = (int)(i & 1);
-    const size_t n = bytes - off < kStageChunk ? bytes - off : kStageChunk;
-    if ((e = cudaEventSynchronize(g_stage.ev[k])) != cudaSuccess) return e;
-    par_memcpy(g_stage.buf[k], static_cast<const char *>(host) + off, n);
-    if ((e = cudaMemcpyAsync(static_cast<char *>(dev) + off, g_stage.buf[k], n, cudaMemcpyHostToDevice, s)) !=
-        cudaSuccess)
-      return e;
-    if ((e = cudaEventRecord(g_stage.ev[k], s)) != cudaSuccess) return e;
-  }
-  for (int k = 0; k < 2; ++k)
-    if ((e = cudaEventSynchronize(g_stage.ev[k])) != cudaSuccess) return e;
-  return cudaSuccess;
-}
-
-// device -> host after the work already issued on s; returns when the host array is filled.
-cudaError_t download(void *host, const void *dev, size_t bytes, cudaStream_t s) {
-  cudaError_t e;
-  if (bytes < (size_t(32) << 20)) {
-    if ((e = cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
-    return cudaStreamSynchronize(s);
-  }
-  if ((e = ensure_staging()) != cudaSuccess) return e;
-  const size_t nchunks = (bytes + kStageChunk - 1) / kStageChunk;
-  // Two chunks in flight: the copy of chunk i+1 overlaps the host copy-out of chunk i.
-  for (size_t i = 0; i < nchunks + 1; ++i) {
-    if (i < nchunks) {
-      const int k = (int)(i & 1);
-      const size_t off = i * kStageChunk, n = bytes - off < kStageChunk ? bytes - off : kStageChunk;
-      if ((e = cudaMemcpyAsync(g_stage.buf[k], static_cast<const char *>(dev) + off, n, cudaMemcpyDeviceToHost, s)) !=
-          cudaSuccess)
-        return e;
-      if ((e = cudaEventRecord(g_stage.ev[k], s)) != cudaSuccess) return e;
-    }
-    if (i > 0) {
-      const size_t j = i - 1;
-      const int k = (int)(j & 1);
-      const size_t off = j * kStageChunk, n = bytes - off < kStageChunk ? bytes - off : kStageChunk;
-      if ((e = cudaEventSynchronize(g_stage.ev[k])) != cudaSuccess) return e;
-      par_memcpy(static_cast<char *>(host) + off, g_stage.buf[k], n);
-    }
-  }
-  return cudaSuccess;
 }
 
 // ---- helpers -------------------------------------------------------------------
@@ -611,7 +524,7 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   } else {
     CK(cudaMalloc(&raw, 6 * g.n * sizeof(float)));
     for (int k = 0; k < 6; ++k) {
-      CK(upload(raw + k * g.n, src6[k], g.n * sizeof(float), s));
+      CK(cudaMemcpyAsync(raw + k * g.n, src6[k], g.n * sizeof(float), cudaMemcpyHostToDevice, s));
       r6.a[k] = raw + k * g.n;
     }
   }
@@ -627,8 +540,8 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
     if (!g.hostmem) {
       // The coefficient kernel has finished with `raw` before these copies
       // (same stream).
-      if (p) CK(upload(raw, p, g.n * sizeof(float), s));
-      if (q) CK(upload(raw + g.n, q, g.n * sizeof(float), s));
+      if (p) CK(cudaMemcpyAsync(raw, p, g.n * sizeof(float), cudaMemcpyHostToDevice, s));
+      if (q) CK(cudaMemcpyAsync(raw + g.n, q, g.n * sizeof(float), cudaMemcpyHostToDevice, s));
       p = p ? raw : nullptr;
       q = q ? raw + g.n : nullptr;
     }
@@ -794,7 +707,7 @@ int read_component(int buf, int comp, float *host) {
     k_unpack<<<grid_for(g.n), 256, 0, g_stream>>>(g.F[buf], out, comp, g.sx, g.sy, g.sz, g.pitch);
     CK(cudaGetLastError());
   }
-  if (!g.hostmem) CK(download(host, g.scratch, g.n * sizeof(float), g_stream));
+  if (!g.hostmem) CK(cudaMemcpyAsync(host, g.scratch, g.n * sizeof(float), cudaMemcpyDeviceToHost, g_stream));
   CK(cudaStreamSynchronize(g_stream));
   return check_err_word();
 }
