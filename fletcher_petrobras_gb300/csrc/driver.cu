@@ -148,18 +148,29 @@ struct Raw6 {
 // terms in FP64.
 __global__ void k_precompute(Raw6 raw, float *__restrict__ coef, int sx, int sy, int sz, int pitch) {
   const size_t n = (size_t)sx * sy * sz;
+  // The trigonometry of the last angles this thread saw: media repeat their
+  // angles over many cells (layers), and the same input gives the same floats.
+  float last_theta = __int_as_float(0x7fbfffff), last_phi = __int_as_float(0x7fbfffff);  // a NaN pattern no input holds
+  float sinTheta = 0.f, cosTheta = 0.f, sin2Theta = 0.f, sinPhi = 0.f, cosPhi = 0.f, sin2Phi = 0.f;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const float vpz = raw.a[0][i], vsv = raw.a[1][i], eps = raw.a[2][i], del = raw.a[3][i];
     const float phi = raw.a[4][i], theta = raw.a[5][i];
-    double st, ct, sp, cp;
-    sincos((double)theta, &st, &ct);
-    sincos((double)phi, &sp, &cp);
-    const float sinTheta = (float)st;
-    const float cosTheta = (float)ct;
-    const float sin2Theta = (float)sin(__dmul_rn(2.0, (double)theta));
-    const float sinPhi = (float)sp;
-    const float cosPhi = (float)cp;
-    const float sin2Phi = (float)sin(__dmul_rn(2.0, (double)phi));
+    if (__float_as_int(theta) != __float_as_int(last_theta)) {
+      double st, ct;
+      sincos((double)theta, &st, &ct);
+      sinTheta = (float)st;
+      cosTheta = (float)ct;
+      sin2Theta = (float)sin(__dmul_rn(2.0, (double)theta));
+      last_theta = theta;
+    }
+    if (__float_as_int(phi) != __float_as_int(last_phi)) {
+      double sp, cp;
+      sincos((double)phi, &sp, &cp);
+      sinPhi = (float)sp;
+      cosPhi = (float)cp;
+      sin2Phi = (float)sin(__dmul_rn(2.0, (double)phi));
+      last_phi = phi;
+    }
     const float v2sz = __fmul_rn(vsv, vsv);
     const float v2pz = __fmul_rn(vpz, vpz);
     const float v2px = (float)__dmul_rn((double)v2pz, __dadd_rn(1.0, __dmul_rn(2.0, (double)eps)));
