@@ -49,7 +49,12 @@ struct GeoH {
   static constexpr int DBUF_B = 2 * TY * HX * 8;
   static constexpr int OFF_H32 = 0;                      // after the stages
   static constexpr int OFF_DB = 2 * H32_B;
-  static constexpr int OFF_BAR = OFF_DB + DBUF_B;
+  // 16-row tiles (512 threads, at most 128 registers) keep the per-cell
+  // in-plane terms (A, B) of the last 5 planes in shared memory.
+  static constexpr bool AB_SMEM = TY >= 16;
+  static constexpr int OFF_AB = OFF_DB + DBUF_B;
+  static constexpr int AB_B = AB_SMEM ? 5 * NT * 16 : 0;
+  static constexpr int OFF_BAR = OFF_AB + AB_B;
   static_assert(TY % 4 == 0, "tile rows must be a multiple of 4");
   static_assert(ARR_B % 128 == 0 && UPD_B % 128 == 0, "stage regions 128-B aligned");
 };
@@ -158,6 +163,7 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
   unsigned char *tail = smem + S * G::STAGE_B;
   f2 *H32 = reinterpret_cast<f2 *>(tail + G::OFF_H32);
   f2 *dbuf = reinterpret_cast<f2 *>(tail + G::OFF_DB);
+  float4 *ABs = reinterpret_cast<float4 *>(tail + G::OFF_AB);  // [5][NT] (AB_SMEM)
   uint64_t *full = reinterpret_cast<uint64_t *>(tail + G::OFF_BAR);
   uint64_t *xchg = full + S;
   int *ctl = reinterpret_cast<int *>(xchg + 1);
@@ -213,6 +219,7 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
   int stage = 0;
   uint32_t phase = 0, xphase = 0;
   int sel = 0;
+  int abw = 0;  // shared A/B ring slot of the arriving plane (the plane 4 back is at abw + 1)
   int pend_z = -1;  // thread 0: plane whose CTA maximum waits in smax[sel ^ 1]
   bool bad = false;
   for (int item = blockIdx.x; item < P.nitems; item += gridDim.x) {
@@ -326,8 +333,17 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
           const float czz = cu[ci], cxz = cu[G::NT + ci], cyz = cu[2 * G::NT + ci];
           const float v2px = cu[3 * G::NT + ci], v2pz = cu[4 * G::NT + ci];
           const float v2sz = cu[5 * G::NT + ci], v2pn = cu[6 * G::NT + ci];
-          const f2 h1 = fma2(splat(cyz), dyz, fma2(splat(cxz), dxz, fma2(splat(czz), d2z, A[cs])));
-          const f2 h2 = sub2(add2(B[cs], d2z), h1);
+          f2 Ak, Bk;
+          if constexpr (G::AB_SMEM) {
+            const float4 ab = ABs[(abw == 4 ? 0 : abw + 1) * G::NT + ci];
+            Ak = mk2(ab.x, ab.y);
+            Bk = mk2(ab.z, ab.w);
+          } else {
+            Ak = A[cs];
+            Bk = B[cs];
+          }
+          const f2 h1 = fma2(splat(cyz), dyz, fma2(splat(cxz), dxz, fma2(splat(czz), d2z, Ak)));
+          const f2 h2 = sub2(add2(Bk, d2z), h1);
           const float h1p = lo(h1), h1q = hi(h1), h2p = lo(h2), h2q = hi(h2);
           const float t = __fmul_rn(v2pz, h1q);
           const float rhsp = __fmaf_rn(v2sz, __fsub_rn(h1p, h1q), __fmaf_rn(v2px, h2p, t));
@@ -366,10 +382,17 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
           const f2 dxy = scale<ISO>(d1(dr[1], dr[-1], dr[2], dr[-2], dr[3], dr[-3], dr[4], dr[-4]), sx1);
           const float *ca = reinterpret_cast<const float *>(st + G::OFF_ARR);
           const float cxx = ca[ci], cyy = ca[G::NT + ci], cxy = ca[2 * G::NT + ci];
-          A[j] = fma2(splat(cxy), dxy, fma2(splat(cyy), d2y, mul2(splat(cxx), d2x)));
-          B[j] = add2(d2x, d2y);
+          const f2 av = fma2(splat(cxy), dxy, fma2(splat(cyy), d2y, mul2(splat(cxx), d2x)));
+          const f2 bv = add2(d2x, d2y);
+          if constexpr (G::AB_SMEM) {
+            ABs[abw * G::NT + ci] = make_float4(lo(av), hi(av), lo(bv), hi(bv));
+          } else {
+            A[j] = av;
+            B[j] = bv;
+          }
         }
         sel ^= 1;
+        abw = abw == 4 ? 0 : abw + 1;
         if (++stage == S) {
           stage = 0;
           phase ^= 1u;
@@ -482,7 +505,7 @@ __global__ void k_half_decode(const unsigned *__restrict__ hv, const unsigned sh
 
 // ---- host side ---------------------------------------------------------------
 
-#define FLT_HALF_SHAPES(X) X(12, 4) X(12, 5) X(12, 6) X(8, 6)
+#define FLT_HALF_SHAPES(X) X(12, 4) X(12, 5) X(12, 6) X(8, 6) X(16, 4) X(16, 5)
 
 template <int TY, int S, bool EXT>
 static cudaError_t launch_half_t(const HalfLaunch &L, cudaStream_t s) {

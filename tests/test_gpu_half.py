@@ -96,7 +96,7 @@ def test_c2_fp32_form_vs_fp64_oracle():
     assert ep < 1e-4 and eq < 1e-4
 
 
-@pytest.mark.parametrize("tile", [(12, 4, 1), (12, 6, 3), (8, 6, 2), (12, 5, 5)])
+@pytest.mark.parametrize("tile", [(12, 4, 1), (12, 6, 3), (8, 6, 2), (12, 5, 5), (16, 5, 0)])
 @pytest.mark.parametrize("form", ["fp16x", "fp16"])
 def test_launch_shapes_bit_identical(form, tile):
     prob = Problem("hshape", 70, 27, 33, absorb=5, dt=0.0006, steps=24, fcut=45.0, kind="layered", layers=5, seed=9)
