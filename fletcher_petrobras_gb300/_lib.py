@@ -26,8 +26,6 @@ SIGNATURES = {
     "FLETCHER_SetStream": (C.c_int, [C.c_void_p]),
     "FLETCHER_GetStream": (C.c_void_p, []),
     "FLETCHER_SetForm": (C.c_int, [C.c_int]),
-    "FLETCHER_SetUniformBlocks": (C.c_int, [C.c_int]),
-    "FLETCHER_ExplicitCoefficientShare": (C.c_double, []),
     "FLETCHER_SetHostAccess": (C.c_int, [C.c_int]),
     "FLETCHER_HostAccess": (C.c_int, []),
     "FLETCHER_SetTileConfig": (C.c_int, [C.c_int, C.c_int, C.c_int]),

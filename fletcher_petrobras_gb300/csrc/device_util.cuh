@@ -97,16 +97,6 @@ __device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *m, uin
       : "memory");
 }
 
-// Plain (untiled) bulk copy global -> shared, completing on `bar`.  Both
-// addresses 16-B aligned, size a multiple of 16.
-__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_addr(dst)),
-      "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
-}
-
 // ---- packed FP32x2 ---------------------------------------------------------
 // A (p, q) pair of one cell travels as one 64-bit register pair; the
 // .f32x2 instructions of sm_100-family parts update both fields at once.

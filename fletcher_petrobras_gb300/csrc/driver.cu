@@ -55,9 +55,6 @@ struct State {
   size_t dev_bytes = 0;
   int num_sms = 0;
   bool hostmem = false;  // kernels read and write the caller's host arrays directly
-  float *utab = nullptr;   // uniform coefficient blocks: one 12-float tuple per (plane, tile)
-  int2 *urange = nullptr;  // per tile, the planes whose coefficients come from utab
-  double explicit_frac = 1.0;  // share of updated cells whose coefficients are loaded per cell
   int form = FLETCHER_FORM_FP32;
   unsigned *Hh[2] = {nullptr, nullptr};
   unsigned short *Hl[2] = {nullptr, nullptr};
@@ -87,7 +84,6 @@ bool g_own_stream = false;
 int g_form = FLETCHER_FORM_FP32;
 int g_req_rows = 0, g_req_stages = 0, g_req_chunks = 0;
 int g_errmode = FLETCHER_ERRMODE_EXIT;
-int g_uniform_blocks = 1;  // detect uniform coefficient blocks (FP32 form)
 // 1: kernels read and write the caller's host arrays where the device
 // supports it; 0 (default): device buffers and copies.  On GB300 with Grace
 // the copies measured faster (e2e 66.3 vs 49.2 GMSamples/s at 504^3).
@@ -227,41 +223,6 @@ __global__ void k_unpack_coef(const float *__restrict__ coef, float *__restrict_
   }
 }
 
-// One block (tile tx, ty of plane z, blockIdx = (tile, z)) of the
-// coefficient volume: does every updated cell hold the same ten values?
-// flag[z * ntiles + tile] = 1 if so (or if the block has no updated cell),
-// and utab gets the values in kernel order (3 arrival, pad, 7 update, pad).
-__global__ void k_uniform_blocks(const float *__restrict__ coef, float *__restrict__ utab,
-                                 unsigned char *__restrict__ flag, int sx, int sy, int sz, int pitch, int bord, int ntx,
-                                 int TY) {
-  const int tile = blockIdx.x, z = blockIdx.y;
-  const int tx = tile % ntx, ty = tile / ntx;
-  const int x0 = kRadius + tx * kTileX, y0 = kRadius + ty * TY;
-  const int xr = max(x0, bord), yr = max(y0, bord);  // the block's first updated cell
-  const bool any = z >= bord && z < sz - bord && xr < min(x0 + kTileX, sx - bord) && yr < min(y0 + TY, sy - bord);
-  const size_t plane = (size_t)sy * pitch, zb = (size_t)z * kNumCoef * plane;
-  const int x = x0 + (int)(threadIdx.x % kTileX), y = y0 + (int)(threadIdx.x / kTileX);
-  const bool valid = any && x >= bord && x < sx - bord && y >= bord && y < sy - bord && y < y0 + TY;
-  bool same = true;
-  if (valid)
-    for (int c = 0; c < kNumCoef; ++c) {
-      const float v = coef[zb + c * plane + (size_t)y * pitch + x];
-      const float r = coef[zb + c * plane + (size_t)yr * pitch + xr];
-      same = same && (__float_as_int(v) == __float_as_int(r));
-    }
-  const bool uni = __syncthreads_and(same);
-  if (threadIdx.x == 0) {
-    const size_t b = (size_t)z * gridDim.x + tile;
-    flag[b] = uni ? 1 : 0;
-    float *t = utab + b * kUniformFloats;
-    for (int c = 0; c < kUniformFloats; ++c) t[c] = 0.f;
-    if (any) {
-      for (int c = 0; c < kArrivalCoef; ++c) t[c] = coef[zb + c * plane + (size_t)yr * pitch + xr];
-      for (int c = 0; c < kUpdateCoef; ++c) t[4 + c] = coef[zb + (kArrivalCoef + c) * plane + (size_t)yr * pitch + xr];
-    }
-  }
-}
-
 // Adds val to both fields of one cell (source outside the fused path).
 __global__ void k_add_source(float2 *F, size_t idx, float val) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
@@ -374,8 +335,6 @@ void free_state() {
     if (g.Hl[b]) cudaFree(g.Hl[b]);
   }
   if (g.E) cudaFree(g.E);
-  if (g.utab) cudaFree(g.utab);
-  if (g.urange) cudaFree(g.urange);
   if (g.Mx) cudaFree(g.Mx);
   if (g.err_host) cudaFreeHost(g.err_host);
   g = State();
@@ -455,60 +414,6 @@ void fill_items(int4 *items, int shot, int ntx, int nty, int nchunk, int TY) {
 
 namespace {
 
-// Uniform coefficient blocks of the FP32 form for tiles of TY rows: per
-// tile, the longest run of planes whose blocks are uniform, and the table of
-// their coefficient tuples.  Bit-identical results: the tuple holds the very
-// values the cells hold.
-int setup_uniform_blocks(int TY) {
-  if (g.utab) cudaFree(g.utab);
-  if (g.urange) cudaFree(g.urange);
-  g.utab = nullptr;
-  g.urange = nullptr;
-  g.explicit_frac = 1.0;
-  if (half_form() || !g_uniform_blocks) return FLETCHER_OK;
-  const int ntiles = g.ntx * g.nty;
-  const size_t nb = (size_t)ntiles * g.sz;
-  unsigned char *dflag = nullptr;
-  CK(cudaMalloc(&g.utab, nb * kUniformFloats * sizeof(float)));
-  CK(cudaMalloc(&g.urange, ntiles * sizeof(int2)));
-  CK(cudaMalloc(&dflag, nb));
-  k_uniform_blocks<<<dim3(ntiles, g.sz), kTileX * TY, 0, g_stream>>>(g.coef, g.utab, dflag, g.sx, g.sy, g.sz, g.pitch,
-                                                                     g.bord, g.ntx, TY);
-  CK(cudaGetLastError());
-  std::vector<unsigned char> flag(nb);
-  CK(cudaMemcpyAsync(flag.data(), dflag, nb, cudaMemcpyDeviceToHost, g_stream));
-  CK(cudaStreamSynchronize(g_stream));
-  cudaFree(dflag);
-  std::vector<int2> range(ntiles);
-  double explicit_cells = 0.0, cells = 0.0;
-  const int depth = g.sz - 2 * g.bord;
-  for (int t = 0; t < ntiles; ++t) {
-    int best0 = 0, best1 = 0, run0 = -1;
-    for (int z = g.bord; z <= g.sz - g.bord; ++z) {
-      const bool u = z < g.sz - g.bord && flag[(size_t)z * ntiles + t];
-      if (u && run0 < 0) run0 = z;
-      if (!u && run0 >= 0) {
-        if (z - run0 > best1 - best0) {
-          best0 = run0;
-          best1 = z;
-        }
-        run0 = -1;
-      }
-    }
-    range[t] = make_int2(best0, best1);
-    const int tx = t % g.ntx, ty = t / g.ntx;
-    const int x0 = kRadius + tx * kTileX, y0 = kRadius + ty * TY;
-    const int vx = std::max(0, std::min(x0 + kTileX, g.sx - g.bord) - std::max(x0, g.bord));
-    const int vy = std::max(0, std::min(y0 + TY, g.sy - g.bord) - std::max(y0, g.bord));
-    cells += (double)vx * vy * depth;
-    explicit_cells += (double)vx * vy * (depth - (best1 - best0));
-  }
-  g.explicit_frac = cells > 0 ? explicit_cells / cells : 1.0;
-  CK(cudaMemcpyAsync(g.urange, range.data(), ntiles * sizeof(int2), cudaMemcpyHostToDevice, g_stream));
-  CK(cudaStreamSynchronize(g_stream));
-  return FLETCHER_OK;
-}
-
 // Tensor maps, work items and the shot descriptor for a tile shape (at
 // initialisation, or between steps: results do not depend on the shape).
 int setup_tiles(int rows, int stages) {
@@ -530,7 +435,7 @@ int setup_tiles(int rows, int stages) {
   g.desc.ntx = g.ntx; g.desc.nty = g.nty; g.desc.chunk = g.chunk;
   g.desc.src_x = g.desc.src_y = g.desc.src_z = -1000;
   g.desc.cor_x = g.desc.cor_y = g.desc.cor_z = -1000;
-  return setup_uniform_blocks(TY);
+  return FLETCHER_OK;
 }
 
 int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, float dt, const float *vpz,
@@ -735,8 +640,6 @@ int step() {
   P.iso = (g.dx == g.dy && g.dx == g.dz) ? 1 : 0;
   P.dt2 = P.iso ? (g.dt * g.dt) * P.inv_dxx : g.dt * g.dt;
   P.err = g.err_dev;
-  P.utab = g.utab;
-  P.urange = g.urange;
   ShotDesc &want = P.one;
   want = g.desc;
   want.src_x = want.src_y = want.src_z = -1000;
@@ -946,26 +849,6 @@ extern "C" int FLETCHER_SetStream(void *s) {
 }
 extern "C" void *FLETCHER_GetStream(void) { return g_stream; }
 
-extern "C" int FLETCHER_SetUniformBlocks(int on) {
-  g_uniform_blocks = on ? 1 : 0;
-  if (g.init && !half_form()) {
-    int rc = 0;
-    if (g_uniform_blocks) {
-      rc = setup_uniform_blocks(g.tile_rows);
-    } else {
-      if (g.utab) cudaFree(g.utab);
-      if (g.urange) cudaFree(g.urange);
-      g.utab = nullptr;
-      g.urange = nullptr;
-      g.explicit_frac = 1.0;
-    }
-    return rc;
-  }
-  return FLETCHER_OK;
-}
-
-extern "C" double FLETCHER_ExplicitCoefficientShare(void) { return g.init ? g.explicit_frac : 1.0; }
-
 extern "C" int FLETCHER_SetHostAccess(int mode) {
   if (mode != 1 && mode != 0) return fail(FLETCHER_ERR_ARGS, "FLETCHER_SetHostAccess: mode must be 0 or 1");
   g_host_access = mode;
@@ -1046,13 +929,9 @@ extern "C" size_t FLETCHER_DeviceBytes(void) { return g.dev_bytes; }
 extern "C" double FLETCHER_BytesPerCell(void) {
   // current (p,q) + previous (p,q) + next (p,q) + ten FP32 coefficients (40 B):
   // 8 B per field pair in FP32, 4 B in FP16, 6 B in FP16X.
-  // With uniform coefficient blocks only the explicit share of the cells
-  // loads its ten coefficients (the tuples are 48 B per 32 x TY block).
   const int form = g.init ? g.form : g_form;
   const double pair = form == FLETCHER_FORM_FP16 ? 4.0 : (form == FLETCHER_FORM_FP16X ? 6.0 : 8.0);
-  const double coef = g.init && g.utab ? 40.0 * g.explicit_frac + (1.0 - g.explicit_frac) * 48.0 / (kTileX * g.tile_rows)
-                                       : 40.0;
-  return 3.0 * pair + coef;
+  return 3.0 * pair + 40.0;
 }
 
 // ---- tile-shape tuning with a configuration file --------------------------------

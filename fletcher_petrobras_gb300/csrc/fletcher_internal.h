@@ -56,16 +56,7 @@ struct PropParams {
   float src;                        // value added at each shot's source cell (src_z >= 0)
   float cor;                        // value owed at each shot's cor cell (cor_z >= 0)
   unsigned int *err;                // error word (bit 0: bounded wait gave up)
-  // Uniform coefficient blocks (single-shot FP32; null: none).  A block is
-  // one tile (32 x TY cells) of one plane whose updated cells share one set
-  // of ten coefficients: utab[block] = 12 floats (the 3 arrival
-  // coefficients, 1 pad, the 7 update ones, 1 pad), block = (z * nty + ty) *
-  // ntx + tx; every plane z in urange[ty * ntx + tx] = [z0, z1) of a tile is
-  // uniform.
-  const float *utab;
-  const int2 *urange;
 };
-constexpr int kUniformFloats = 12;
 
 // The four descriptors a single-shot launch passes as kernel parameters.
 struct SingleMaps {

@@ -68,8 +68,6 @@ constexpr size_t smem_bytes() {
 struct Item {
   int x0, y0, z0, z1;
   int shot;
-  int blk;       // tile index ty * ntx + tx (single shot)
-  int zu0, zu1;  // planes whose coefficients come from the uniform-block table
 };
 
 template <int TY, bool BATCH>
@@ -83,8 +81,6 @@ __device__ __forceinline__ Item decode_item(int item, const PropParams &P) {
     it.z0 = d.bord + w.w * d.chunk;
     it.z1 = min(it.z0 + d.chunk, d.sz - d.bord);
     it.shot = w.x;
-    it.blk = 0;
-    it.zu0 = it.zu1 = 0;
   } else {
     const ShotDesc &d = P.one;
     const int tx = item % d.ntx;
@@ -96,14 +92,6 @@ __device__ __forceinline__ Item decode_item(int item, const PropParams &P) {
     it.z0 = d.bord + ch * d.chunk;
     it.z1 = min(it.z0 + d.chunk, d.sz - d.bord);
     it.shot = 0;
-    it.blk = ty * d.ntx + tx;
-    if (P.urange) {
-      const int2 r = P.urange[it.blk];
-      it.zu0 = r.x;
-      it.zu1 = r.y;
-    } else {
-      it.zu0 = it.zu1 = 0;
-    }
   }
   return it;
 }
@@ -120,35 +108,20 @@ struct Cursor {
   int item, k, stage;
 };
 
-// Issues the TMA loads of one step (plane k of item `it`) into `stage`.  In
-// a uniform block the 3 (or 7) coefficients arrive as one 16 (32) B tuple
-// from the uniform-block table instead of a coefficient tile.
+// Issues the TMA loads of one step (plane k of item `it`) into `stage`.
 template <int TY>
 __device__ __forceinline__ void issue_step(unsigned char *stage, uint64_t *bar, const Item &it, int k,
-                                           const StepMaps &m, const PropParams &P) {
+                                           const StepMaps &m) {
   using G = Geo<TY>;
   const bool center = (k >= it.z0) && (k < it.z1);
-  const int ku = k - kRadius;
-  const bool upd = (ku >= it.z0);
-  const bool ua = center && k >= it.zu0 && k < it.zu1;
-  const bool uu = upd && ku >= it.zu0 && ku < it.zu1;
-  const uint32_t bytes = G::HALO_B + (center ? (ua ? 16u : (uint32_t)G::ARR_B) : 0u) +
-                         (upd ? (uu ? 32u : (uint32_t)G::UPD_B) + G::PP_B : 0u);
+  const bool upd = (k - kRadius >= it.z0);
+  const uint32_t bytes = G::HALO_B + (center ? G::ARR_B : 0) + (upd ? G::UPD_B + G::PP_B : 0);
   mbar_arrive_expect_tx(bar, bytes);
   tma_load_3d(stage, m.cur, bar, it.x0 - kRadius, it.y0 - kRadius, k);
-  const size_t nblk = (size_t)P.one.ntx * P.one.nty;
-  if (center) {
-    if (ua)
-      bulk_load(stage + G::OFF_ARR, P.utab + ((size_t)k * nblk + it.blk) * kUniformFloats, 16, bar);
-    else
-      tma_load_4d(stage + G::OFF_ARR, m.arr, bar, it.x0, it.y0, 0, k);
-  }
+  if (center) tma_load_4d(stage + G::OFF_ARR, m.arr, bar, it.x0, it.y0, 0, k);
   if (upd) {
-    if (uu)
-      bulk_load(stage + G::OFF_UPD, P.utab + ((size_t)ku * nblk + it.blk) * kUniformFloats + 4, 32, bar);
-    else
-      tma_load_4d(stage + G::OFF_UPD, m.upd, bar, it.x0, it.y0, kArrivalCoef, ku);
-    tma_load_3d(stage + G::OFF_PP, m.prev, bar, it.x0, it.y0, ku);
+    tma_load_4d(stage + G::OFF_UPD, m.upd, bar, it.x0, it.y0, kArrivalCoef, k - kRadius);
+    tma_load_3d(stage + G::OFF_PP, m.prev, bar, it.x0, it.y0, k - kRadius);
   }
 }
 
@@ -212,7 +185,7 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   // Issues the cursor's step into its stage and advances the cursor.
   auto produce = [&]() {
     Cursor c = *cur;
-    issue_step<TY>(smem + c.stage * G::STAGE_B, &full[c.stage], c.it, c.k, maps_of(c.it), P);
+    issue_step<TY>(smem + c.stage * G::STAGE_B, &full[c.stage], c.it, c.k, maps_of(c.it));
     if (++c.stage == S) c.stage = 0;
     if (++c.k >= c.it.z1 + kRadius) {
       c.item += gridDim.x;
@@ -368,13 +341,10 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
 #undef RP
 #undef RX
 #undef RY
-          // Coefficient c of this cell: tile[c * NT + ci], or tuple[c] in a uniform block.
-          const bool uu = (k - kRadius >= it.zu0) && (k - kRadius < it.zu1);
-          const int uo = uu ? 0 : ci, us = uu ? 1 : G::NT;
-          const float *cu = reinterpret_cast<const float *>(st + G::OFF_UPD) + uo;
-          const float czz = cu[0], cxz = cu[us], cyz = cu[2 * us];
-          const float v2px = cu[3 * us], v2pz = cu[4 * us];
-          const float v2sz = cu[5 * us], v2pn = cu[6 * us];
+          const float *cu = reinterpret_cast<const float *>(st + G::OFF_UPD);
+          const float czz = cu[ci], cxz = cu[G::NT + ci], cyz = cu[2 * G::NT + ci];
+          const float v2px = cu[3 * G::NT + ci], v2pz = cu[4 * G::NT + ci];
+          const float v2sz = cu[5 * G::NT + ci], v2pn = cu[6 * G::NT + ci];
           f2 Ak, Bk;
           if constexpr (G::AB_SMEM) {
             const float4 ab = ABs[(abw == 4 ? 0 : abw + 1) * G::NT + ci];
@@ -411,10 +381,8 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
         if (center) {
           const f2 *dr = db + ly * G::HX + lx + kRadius;
           const f2 dxy = scale<ISO>(d1(dr[1], dr[-1], dr[2], dr[-2], dr[3], dr[-3], dr[4], dr[-4]), sx1);
-          const bool ua = (k >= it.zu0) && (k < it.zu1);
-          const int ao = ua ? 0 : ci, as = ua ? 1 : G::NT;
-          const float *ca = reinterpret_cast<const float *>(st + G::OFF_ARR) + ao;
-          const float cxx = ca[0], cyy = ca[as], cxy = ca[2 * as];
+          const float *ca = reinterpret_cast<const float *>(st + G::OFF_ARR);
+          const float cxx = ca[ci], cyy = ca[G::NT + ci], cxy = ca[2 * G::NT + ci];
           const f2 av = fma2(splat(cxy), dxy, fma2(splat(cyy), d2y, mul2(splat(cxx), d2x)));
           const f2 bv = add2(d2x, d2y);
           if constexpr (G::AB_SMEM) {

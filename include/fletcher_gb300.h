@@ -80,17 +80,6 @@ void FLETCHER_ClearError(void);
 int FLETCHER_SetStream(void *cuda_stream);
 void *FLETCHER_GetStream(void);
 
-/* Uniform coefficient blocks (FP32 form; on by default).  After the
- * coefficient precompute, every tile (32 x tile-rows cells) of every plane
- * whose updated cells share one set of ten coefficients is found; over each
- * tile's longest run of such planes the kernel loads one 48-byte tuple per
- * block instead of 40 bytes per cell.  The values are the same, so results
- * are bit-identical.  FLETCHER_SetUniformBlocks(0) turns it off (applies at
- * once to an initialised state); FLETCHER_ExplicitCoefficientShare() is the
- * share of updated cells that still load their coefficients per cell. */
-int FLETCHER_SetUniformBlocks(int on);
-double FLETCHER_ExplicitCoefficientShare(void);
-
 /* Host arrays.  By default DRIVER_Initialize copies the caller's model and
  * field arrays to device buffers, and read-backs copy to the caller's
  * arrays.  FLETCHER_SetHostAccess(1), before DRIVER_Initialize, lets the

@@ -283,32 +283,3 @@ def test_host_access_and_copy_paths_identical():
     assert modes[1] == 0
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a, b)
-
-
-@pytest.mark.parametrize("kind", ["layered", "homogeneous", "random_cells"])
-def test_uniform_coefficient_blocks_bit_identical(kind):
-    """Coefficients from the uniform-block table (one tuple per tile and
-    plane) give the same floats as the per-cell coefficient tiles."""
-    prob = Problem("ublk", 70, 40, 36, absorb=6, dt=0.0006, steps=25, fcut=45.0, kind="homogeneous"
-                   if kind == "homogeneous" else "layered", layers=4, seed=3)
-    prob = prob.with_(source=(prob.sx // 2, prob.sy // 2, prob.sz // 2))
-    m = prob.model()
-    if kind == "random_cells":  # a few scattered cells break some blocks
-        g = np.random.default_rng(1)
-        idx = g.choice(prob.n, 40, replace=False)
-        m[2][idx] = m[2][idx] * np.float32(1.01)
-    out, shares = [], []
-    for on in (1, 0):
-        prop = Propagator()
-        prop.lib.FLETCHER_SetUniformBlocks(on)
-        prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, m)
-        shares.append(prop.lib.FLETCHER_ExplicitCoefficientShare())
-        prop.run(prob.steps, prob.i_source, prob.sources())
-        prop.synchronize()
-        out.append([prop.field(k) for k in range(4)])
-        prop.finalize()
-    Propagator().lib.FLETCHER_SetUniformBlocks(1)
-    print(kind, "explicit share", shares)
-    assert shares[1] == 1.0 and 0.0 <= shares[0] < 1.0
-    for a, b in zip(out[0], out[1]):
-        assert np.array_equal(a, b)
