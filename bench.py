@@ -394,7 +394,8 @@ def run_learned_form(args, ws, rank, local, group):
     loss = learned.train(iters=3000, batch=8192, lr=3e-3)
     t2 = time.time()
     n, steps = args.abc_interior, args.abc_steps
-    res = learned.compare(n=n, steps=steps, nsnap=5)
+    res = learned.compare(n=n, steps=steps, nsnap=5,
+                          kinds=("random", "learned", "learned@2", "learned@4", "oneway", "plain8"))
     group.barrier()
     if rank != 0:
         return
@@ -409,7 +410,7 @@ def run_learned_form(args, ws, rank, local, group):
         forms[k] = {"interior_msamples": round(v["interior_msamples"], 1), "ms_per_step": round(v["ms_per_step"], 4),
                     "reflected_energy": fin(v["reflected_energy"]),
                     "reflected_energy_by_snapshot": [fin(e) for e in v.get("reflected_energy_by_snapshot", [])],
-                    "launches_per_step": v.get("launches_per_step", 1)}
+                    "launches_per_step": v.get("launches_per_step", 1), "tile": v.get("tile")}
     lv, rv = res["learned"], res["random"]
     line = {
         "metric": "interior MSamples/s, learned 8-cell layer vs 32-cell random boundary (C4)",
@@ -417,8 +418,10 @@ def run_learned_form(args, ws, rank, local, group):
         "higher_is_better": True, "scaling": "weak", "dtype": "f32 (network: f16 weights, f32 accumulation)",
         "data": "synthetic (seeded layered TTI models)",
         "config": {"workload": f"C4: {n}^3 interior, {steps} steps, dt 0.6 ms, 15 Hz Ricker 8 cells below the "
-                               "interior top; forms: learned 8-cell layer, 32-cell random-velocity shell, bare 8-cell "
-                               "layer (plain8), 8-cell taper (sponge), wide reflection-free reference",
+                               "interior top; forms: learned 8-cell layer (one-way update of its outer 4 cells with "
+                               "the network's coefficients), the same with the medium's coefficients (oneway), "
+                               "32-cell random-velocity shell, bare 8-cell layer (plain8), wide reflection-free "
+                               "reference",
                    "snapshots": res["snapshots"],
                    "training": {"models": 64, "samples": ns, "collect_s": round(t1 - t0, 1),
                                 "train_s": round(t2 - t1, 1), "iters": 3000, "batch": 8192,
@@ -426,6 +429,7 @@ def run_learned_form(args, ws, rank, local, group):
         "speedup_vs_random": round(rv["ms_per_step"] / lv["ms_per_step"], 3),
         "reflected_energy_learned": fin(lv["reflected_energy"]),
         "reflected_energy_random": fin(rv["reflected_energy"]),
+        "reflected_energy_oneway": fin(res["oneway"]["reflected_energy"]) if "oneway" in res else None,
         "learned_stable": fin(lv["reflected_energy"]) is not None and lv["reflected_energy"] < 1.0,
         "forms": forms,
     }

@@ -68,8 +68,8 @@ SIGNATURES = {
     "FLETCHER_SliceFrames": (C.c_int, [C.c_void_p]),
     "FLETCHER_DumpSliceSummary": (C.c_int, [C.c_int] * 3 + [C.c_void_p, C.c_float, C.c_int, FP, C.c_float]),
     "FLETCHER_AbcInit": (C.c_int, [C.c_uint]),
-    "FLETCHER_AbcSetWeights": (C.c_int, [FP, C.c_float]),
-    "FLETCHER_AbcGetWeights": (C.c_int, [FP, FP]),
+    "FLETCHER_AbcSetWeights": (C.c_int, [FP]),
+    "FLETCHER_AbcGetWeights": (C.c_int, [FP]),
     "FLETCHER_AbcReserve": (C.c_int, [C.c_long]),
     "FLETCHER_AbcCollect": (C.c_int, [IP, IP, C.c_int, C.c_float, C.c_uint, C.c_float]),
     "FLETCHER_AbcSamples": (C.c_long, []),
@@ -78,7 +78,9 @@ SIGNATURES = {
     "FLETCHER_AbcGradient": (C.c_int, [FP, FP, C.c_int, FP, FP]),
     "FLETCHER_AbcForward": (C.c_int, [FP, C.c_int, FP]),
     "FLETCHER_SetBoundary": (C.c_int, [C.c_int, C.c_int, C.c_float]),
+    "FLETCHER_PlanSegments": (C.c_int, [C.c_int] * 7 + [IP, C.c_int, IP, C.POINTER(C.c_long)]),
     "FLETCHER_AbcLayerCells": (C.c_long, []),
+    "FLETCHER_AbcSetInterval": (C.c_int, [C.c_int]),
     "FLETCHER_AbcRelease": (None, []),
 }
 

@@ -1,34 +1,53 @@
 // Learned absorbing boundary: a thin layer around the interior whose outer
-// cells get a correction from a small per-cell MLP.
+// cells are advanced by a one-way (outgoing-wave) update with a per-cell
+// coefficient predicted by a small MLP.
 //
 // Geometry.  The grid is interior + a layer of L cells + bord zero cells on
 // every side; the plain update runs over interior and layer alike (the
-// medium is extended into the layer, no random velocities).  A layer cell at
-// Chebyshev distance d outside the interior has an update stencil (radius 4)
-// that reaches past the layer once d > L - 4; those reads see the zero
-// border where an unbounded medium would hold the outgoing wave.  The
-// network predicts the missing part of the update, dt^2 * rhs(field beyond
-// the layer) (the rhs of original/sample.h:32-89), from what the cell can
-// see: the 9-point stencils of p and q along its outward normal at t and
-// t-1 (points beyond the layer read as zero), vpz, epsilon, delta and d / L.
-// Stencil inputs are divided by their largest magnitude s and the output is
-// multiplied by s * out_scale, so the network works on unit-scale values.
-// It serves the face cells of the layer (one axis more than L - 4 outside);
-// edge and corner cells keep the plain update.
+// medium is extended into the layer, no random velocities).  A layer cell d
+// cells outside the interior along an axis has an update stencil (radius 4)
+// reaching d + 4 cells out; for the layer's outer 4 cells (d = L-3 .. L,
+// the ghost zone) that reaches the zero border, where an unbounded medium
+// would hold the outgoing wave.  After the plain step those cells are
+// overwritten with the box-scheme update of the one-way wave equation
+// u_t + c u_n = 0 along the outward normal n,
+//
+//     u_g(t+1) = u_i(t) + k (u_g(t) - u_i(t+1)),   k = (1 - r) / (1 + r),  r = c dt / h
+//
+// (g the ghost cell, i its inward neighbour), applied outward from d = L-3
+// (whose inward neighbour carries the plain update) to d = L, for p and q,
+// face by face: the z faces, then the y faces, then the x faces (edge and
+// corner cells keep the last face's value).  For r > 0 the box scheme of
+// the one-way equation is unconditionally stable and 0 < k < 1.
+//
+//  * FLETCHER_BOUNDARY_ONEWAY: k from the medium, c = vpz along z and
+//    vpz sqrt(1 + 2 epsilon) along x and y (the normal-incidence P-wave
+//    velocities of a vertical-axis medium);
+//  * FLETCHER_BOUNDARY_LEARNED: (k_p, k_q) = sigmoid(network(inputs)) per
+//    ghost cell and step.  The inputs are the 9-point stencils of p and q
+//    along the outward normal at t and t-1 (points beyond the layer read as
+//    zero) divided by their largest magnitude s, vpz / 4000, epsilon, delta
+//    and d / L; the network learns the coefficient with which the update
+//    reproduces the unbounded medium's next value (oblique incidence,
+//    tilted anisotropy, the wave's own apparent velocity).
 //
 // Network: 40 -> 32 -> 32 -> 2, tanh, FP16 weights and FP16 activations
 // between layers, FP32 accumulation and FP32 biases.
 //   * inference (k_abc_infer) runs on the tensor cores (mma.sync m16n8k16,
-//     f16 x f16 -> f32): one warp evaluates 16 cells, the layer-1 and
+//     f16 x f16 -> f32): one warp evaluates 16 ghost cells, the layer-1 and
 //     layer-2 outputs stay in registers as the next layer's A fragments;
 //   * training (k_abc_train) is a per-sample forward and backward pass in
 //     FP32 with the same roundings (straight-through), block sums of the
-//     gradients, and Adam (k_abc_adam) on FP32 master weights.
+//     gradients, and Adam (k_abc_adam) on FP32 master weights.  The loss of
+//     a sample is sum_c (sigmoid(y_c) a_c - b_c)^2 with a = (u_g(t) -
+//     u_i(t+1)) / s and b = (u_g(t+1) - u_i(t)) / s: the update's error
+//     when the neighbour's next value is the true one.
 //
 // Training data (k_abc_collect) come from plain-method runs on padded
-// domains: around a virtual interior box, the layer cells' inputs are read
-// with everything beyond the layer set to zero, and the target is the
-// update's contribution from the cells beyond the layer.
+// domains: around a virtual interior box, the ghost cells' inputs are read
+// with everything beyond the virtual layer set to zero, and the next values
+// u(t+1) are the plain update on the padded field (an unbounded medium as
+// far as the ghost cells can tell).
 #include <cuda_fp16.h>
 #include <math.h>
 #include <stdint.h>
@@ -46,7 +65,8 @@ int flt_record_error(int code, const char *msg);
 namespace flt {
 
 constexpr int kIn = 40, kHid = 32, kOut = 2;
-constexpr int kSt = 36;  // stencil inputs (4 x 9)
+constexpr int kTgt = 4;   // targets of a sample: a_p, a_q, b_p, b_q
+constexpr int kSt = 36;   // stencil inputs (4 x 9)
 // Master parameter layout (FP32): W1 [32][40], b1, W2 [32][32], b2, W3 [2][32], b3.
 constexpr int oW1 = 0, oB1 = oW1 + kHid * kIn, oW2 = oB1 + kHid, oB2 = oW2 + kHid * kHid, oW3 = oB2 + kHid,
               oB3 = oW3 + kOut * kHid, kNP = oB3 + kOut;
@@ -55,6 +75,8 @@ constexpr int kK1 = 48;      // layer-1 K padded to a multiple of 16
 constexpr int kXs = 56;      // row stride (halves) of a warp's feature tile: conflict-free A loads
 constexpr float kVScale = 1.0f / 4000.0f;
 constexpr float kMinScale = 1e-30f;  // smallest stencil magnitude the network sees
+constexpr int kGhostD = kRadius;     // ghost cells per ray: the layer's outer 4
+constexpr float kInitBias = 0.85f;   // initial output bias: k ~ 0.7 (r ~ 0.18)
 
 // Inference copy of the network: FP16 weights in mma B-operand order
 // (row n = output, contiguous k), FP32 biases.
@@ -63,14 +85,6 @@ struct NetHalf {
   __half w2[kHid * kHid];
   __half w3[8 * kHid];
   float b1[kHid], b2[kHid], b3[8];
-  float out_scale;
-};
-
-// One layer cell: position, outward axis (0 x, 1 y, 2 z), direction
-// (+1 / -1), distance d, and its medium.
-struct LayerCell {
-  int x, y, z, code;  // code = axis | (sign > 0) << 2 | d << 3
-  float vpz, eps, del, pad;
 };
 
 // A box [lo, hi) per axis.
@@ -78,8 +92,86 @@ struct Box {
   int lo[3], hi[3];
 };
 
+// One layer cell (the taper's list): position and distance d.
+struct LayerCell {
+  int x, y, z, d;
+};
+
+// The ghost zone of a layer: the interior box, the layer, the kept box
+// (interior grown by L) and the first cell of each face.  Faces 0..5 are
+// z-, z+, y-, y+, x-, x+; a face is a set of rays along its outward normal,
+// one per transverse position of the kept box (first transverse axis
+// fastest), 4 cells per ray (d = L-3 .. L, d fastest).
+struct Ghost {
+  Box in, keep;
+  int L;
+  long off[7];
+};
+
+__host__ __device__ __forceinline__ int face_axis(int f) { return 2 - f / 2; }
+__host__ __device__ __forceinline__ int face_sign(int f) { return (f & 1) ? 1 : -1; }
+__host__ __device__ __forceinline__ void transverse(int a, int &t0, int &t1) {
+  t0 = a == 0 ? 1 : 0;
+  t1 = a == 2 ? 1 : 2;
+}
+
+Ghost make_ghost(const Box &in, int L) {
+  Ghost G;
+  G.in = in;
+  G.L = L;
+  for (int a = 0; a < 3; ++a) {
+    G.keep.lo[a] = in.lo[a] - L;
+    G.keep.hi[a] = in.hi[a] + L;
+  }
+  G.off[0] = 0;
+  for (int f = 0; f < 6; ++f) {
+    int t0, t1;
+    transverse(face_axis(f), t0, t1);
+    const long rays = (long)(G.keep.hi[t0] - G.keep.lo[t0]) * (G.keep.hi[t1] - G.keep.lo[t1]);
+    G.off[f + 1] = G.off[f] + rays * kGhostD;
+  }
+  return G;
+}
+
+// Ghost cell i: coordinates c, face f, normal axis a, outward sign; returns d.
+__host__ __device__ __forceinline__ int ghost_cell(const Ghost &G, long i, int (&c)[3], int &f, int &a, int &sgn) {
+  f = 0;
+  while (f < 5 && i >= G.off[f + 1]) ++f;
+  const long j = i - G.off[f];
+  a = face_axis(f);
+  sgn = face_sign(f);
+  int t0, t1;
+  transverse(a, t0, t1);
+  const int e0 = G.keep.hi[t0] - G.keep.lo[t0];
+  const int ray = (int)(j / kGhostD);  // a face holds fewer than 2^31 rays
+  const int d = G.L - kGhostD + 1 + (int)(j % kGhostD);
+  c[t0] = G.keep.lo[t0] + ray % e0;
+  c[t1] = G.keep.lo[t1] + ray / e0;
+  c[a] = sgn < 0 ? G.in.lo[a] - d : G.in.hi[a] - 1 + d;
+  return d;
+}
+
+__host__ __device__ __forceinline__ int face_of(const Ghost &G, long i) {
+  int f = 0;
+  while (f < 5 && i >= G.off[f + 1]) ++f;
+  return f;
+}
+
+// Index step of one cell outward along face f's normal.
+__host__ __device__ __forceinline__ int normal_step(int f, int sy, int pitch) {
+  const int a = face_axis(f);
+  const int s = a == 0 ? 1 : (a == 1 ? pitch : sy * pitch);
+  return face_sign(f) > 0 ? s : -s;
+}
+
+__host__ __device__ __forceinline__ long cell_index(int x, int y, int z, int sy, int pitch) {
+  return ((long)z * sy + y) * pitch + x;
+}
+
 // ---- features -------------------------------------------------------------------
 
+// vpz, epsilon, delta of a cell from its coefficients (v2pz = vpz^2,
+// v2px = vpz^2 (1 + 2 eps), v2pn = vpz^2 (1 + 2 delta): original/precomp.h).
 __device__ __forceinline__ float4 medium_of(const float *coef, int x, int y, int z, int sy, int pitch) {
   const size_t plane = (size_t)sy * pitch, row = (size_t)y * pitch + x;
   const size_t base = (size_t)z * kNumCoef * plane + row;
@@ -104,44 +196,21 @@ __device__ __forceinline__ void normal_stencil(const float2 *F, int x, int y, in
     float2 v = make_float2(0.f, 0.f);
     if (c[0] >= keep.lo[0] && c[0] < keep.hi[0] && c[1] >= keep.lo[1] && c[1] < keep.hi[1] && c[2] >= keep.lo[2] &&
         c[2] < keep.hi[2])
-      v = F[((size_t)c[2] * sy + c[1]) * pitch + c[0]];
+      v = F[cell_index(c[0], c[1], c[2], sy, pitch)];
     p9[j + kRadius] = v.x;
     q9[j + kRadius] = v.y;
   }
 }
 
-// Distance outside `in` (Chebyshev), outward axis (first largest) and sign.
-__host__ __device__ __forceinline__ int outside_of(const Box &in, int x, int y, int z, int *axis, int *sgn) {
-  const int c[3] = {x, y, z};
-  int d = 0, a = 0, s = 1;
-  for (int k = 0; k < 3; ++k) {
-    const int lo = in.lo[k] - c[k], hi = c[k] - (in.hi[k] - 1);
-    const int dk = lo > hi ? lo : hi;
-    if (dk > d) {
-      d = dk;
-      a = k;
-      s = hi > 0 ? 1 : -1;
-    }
-  }
-  *axis = a;
-  *sgn = s;
-  return d;
+// One-way coefficient of the medium along axis a: k = (1 - r) / (1 + r),
+// r = c dt / h, c = vpz (z) or vpz sqrt(1 + 2 eps) (x, y).
+__host__ __device__ __forceinline__ float oneway_k(float vpz, float eps, int a, float dt, float h) {
+  const float c = a == 2 ? vpz : vpz * sqrtf(1.0f + 2.0f * eps);
+  const float r = c * dt / h;
+  return (1.0f - r) / (1.0f + r);
 }
 
-// Number of axes along which (x, y, z) lies more than L - 4 cells outside
-// `in` (its stencil along that axis reaches past the layer).  The network
-// serves face cells (exactly one such axis); its input sees one normal.
-__host__ __device__ __forceinline__ int far_axes(const Box &in, int x, int y, int z, int L) {
-  const int c[3] = {x, y, z};
-  int n = 0;
-  for (int k = 0; k < 3; ++k) {
-    const int lo = in.lo[k] - c[k], hi = c[k] - (in.hi[k] - 1);
-    n += (lo > L - kRadius || hi > L - kRadius) ? 1 : 0;
-  }
-  return n;
-}
-
-// ---- targets: the update's contribution of the cells outside `keep` ----
+// ---- the plain update's rhs over the cells outside a box (an empty box: every cell) ----
 
 // (p, q) of the current field at a cell, if it lies outside `keep`.
 __device__ __forceinline__ float2 outer(const float2 *F, int x, int y, int z, const Box &keep, int sy, int pitch) {
@@ -152,12 +221,17 @@ __device__ __forceinline__ float2 outer(const float2 *F, int x, int y, int z, co
 }
 
 // dt^2 * (rhsp, rhsq) of original/sample.h:32-89 evaluated on the field
-// outside `keep` (it is linear in the field).
+// outside `keep` (it is linear in the field; an empty `keep` gives the
+// whole update).
 __device__ float2 outer_update(const float2 *F, const float *coef, int x, int y, int z, const Box &keep, int sy,
                                int pitch, float dx, float dy, float dz, float dt) {
   const float K[5] = {cK0, cK1, cK2, cK3, cK4};
   const float Lw[5] = {0.f, cL1, cL2, cL3, cL4};
-  float2 d2[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  // The centre term counts when the cell itself lies outside `keep`.
+  const float2 u0 = outer(F, x, y, z, keep, sy, pitch);
+  float2 d2[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) d2[a] = make_float2(K[0] * u0.x, K[0] * u0.y);
   const int cx[3] = {1, 0, 0}, cy[3] = {0, 1, 0}, cz[3] = {0, 0, 1};
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -213,45 +287,53 @@ __device__ __forceinline__ uint32_t mix32(uint32_t a, uint32_t b) {
   return h;
 }
 
-// Training samples from the face cells of the layer of a virtual interior
-// box `in` (layer L, keep = in grown by L): features, targets / s and the
-// cell.  A random fraction `keep_frac` of the cells is taken; cells whose
-// stencils are below `min_scale` carry no wave and are skipped.
-__global__ void k_abc_collect(const float2 *cur, const float2 *prev, const float *coef, Box in, Box keep, int L,
-                              int sy, int pitch, float dx, float dy, float dz, float dt, float keep_frac,
-                              uint32_t seed, float min_scale, float *feat, float *tgt, int4 *pos,
-                              unsigned long long *count, unsigned long long cap) {
-  const int ex = keep.hi[0] - keep.lo[0], ey = keep.hi[1] - keep.lo[1], ez = keep.hi[2] - keep.lo[2];
-  const long n = (long)ex * ey * ez;
+// Training samples from the ghost cells of the layer around a virtual
+// interior box: features, targets (a_p, a_q, b_p, b_q) over s, and the
+// cell (x, y, z, face + 8 d).  A random fraction `keep_frac` of the cells is
+// taken; cells whose stencils are below `min_scale` carry no wave and are
+// skipped.  The next values are the plain update of original/sample.h:32-89
+// (u(t+1) = 2 u(t) - u(t-1) + dt^2 rhs) on the padded field.
+__global__ void k_abc_collect(const float2 *cur, const float2 *prev, const float *coef, const __grid_constant__ Ghost G, int sy, int pitch,
+                              float dx, float dy, float dz, float dt, float keep_frac, uint32_t seed, float min_scale,
+                              float *feat, float *tgt, int4 *pos, unsigned long long *count, unsigned long long cap) {
+  const long n = G.off[6];
+  const Box all = {{0, 0, 0}, {0, 0, 0}};  // empty kept box: the whole field counts
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const int x = keep.lo[0] + (int)(i % ex), y = keep.lo[1] + (int)((i / ex) % ey),
-              z = keep.lo[2] + (int)(i / ((long)ex * ey));
-    int a, sgn;
-    const int d = outside_of(in, x, y, z, &a, &sgn);
-    if (d <= L - kRadius || far_axes(in, x, y, z, L) != 1) continue;
     if ((mix32(seed, (uint32_t)i) >> 8) * (1.0f / 16777216.0f) >= keep_frac) continue;
+    int c[3], f, a, sgn;
+    const int d = ghost_cell(G, i, c, f, a, sgn);
     float v[kSt];
-    normal_stencil(cur, x, y, z, a, sgn, keep, sy, pitch, v, v + 9);
-    normal_stencil(prev, x, y, z, a, sgn, keep, sy, pitch, v + 18, v + 27);
+    normal_stencil(cur, c[0], c[1], c[2], a, sgn, G.keep, sy, pitch, v, v + 9);
+    normal_stencil(prev, c[0], c[1], c[2], a, sgn, G.keep, sy, pitch, v + 18, v + 27);
     float s = 0.f;
 #pragma unroll
     for (int k = 0; k < kSt; ++k) s = fmaxf(s, fabsf(v[k]));
     if (!(s > min_scale) || !(s > kMinScale)) continue;
     const unsigned long long slot = atomicAdd(count, 1ull);
     if (slot >= cap) continue;
-    pos[slot] = make_int4(x, y, z, d);
+    pos[slot] = make_int4(c[0], c[1], c[2], f + 8 * d);
     const float inv = 1.0f / s;
-    float *f = feat + slot * kIn;
+    float *fr = feat + slot * kIn;
 #pragma unroll
-    for (int k = 0; k < kSt; ++k) f[k] = v[k] * inv;
-    const float4 m = medium_of(coef, x, y, z, sy, pitch);
-    f[36] = m.x * kVScale;
-    f[37] = m.y;
-    f[38] = m.z;
-    f[39] = (float)d / (float)L;
-    const float2 t = outer_update(cur, coef, x, y, z, keep, sy, pitch, dx, dy, dz, dt);
-    tgt[slot * 2] = t.x * inv;
-    tgt[slot * 2 + 1] = t.y * inv;
+    for (int k = 0; k < kSt; ++k) fr[k] = v[k] * inv;
+    const float4 m = medium_of(coef, c[0], c[1], c[2], sy, pitch);
+    fr[36] = m.x * kVScale;
+    fr[37] = m.y;
+    fr[38] = m.z;
+    fr[39] = (float)d / (float)G.L;
+    int ci[3] = {c[0], c[1], c[2]};
+    ci[a] -= sgn;
+    const long g = cell_index(c[0], c[1], c[2], sy, pitch), gi = cell_index(ci[0], ci[1], ci[2], sy, pitch);
+    const float2 ug = cur[g], ui = cur[gi], ugm = prev[g], uim = prev[gi];
+    const float2 rg = outer_update(cur, coef, c[0], c[1], c[2], all, sy, pitch, dx, dy, dz, dt);
+    const float2 ri = outer_update(cur, coef, ci[0], ci[1], ci[2], all, sy, pitch, dx, dy, dz, dt);
+    const float ugx = 2.0f * ug.x - ugm.x + rg.x, ugy = 2.0f * ug.y - ugm.y + rg.y;
+    const float uix = 2.0f * ui.x - uim.x + ri.x, uiy = 2.0f * ui.y - uim.y + ri.y;
+    float *t = tgt + slot * kTgt;
+    t[0] = (ug.x - uix) * inv;
+    t[1] = (ug.y - uiy) * inv;
+    t[2] = (ugx - ui.x) * inv;
+    t[3] = (ugy - ui.y) * inv;
   }
 }
 
@@ -265,15 +347,17 @@ __device__ __forceinline__ void mma16816(float (&c)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-__device__ __forceinline__ float tanh_fast(float x) {
-  float y;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-
 __device__ __forceinline__ uint32_t pack_h2(float lo_v, float hi_v) {
   const __half2 h = __floats2half2_rn(lo_v, hi_v);
   return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+// tanh of two pre-activations, rounded to FP16 first, as one packed
+// half2 tanh.approx (the activations feed the next MMA as FP16 anyway).
+__device__ __forceinline__ uint32_t tanh_h2(float lo_v, float hi_v) {
+  uint32_t x = pack_h2(lo_v, hi_v), y;
+  asm("tanh.approx.f16x2 %0, %1;" : "=r"(y) : "r"(x));
+  return y;
 }
 
 // The network on the warp's 16-row feature tile Xs (FP16, row stride kXs).
@@ -302,10 +386,10 @@ __device__ __forceinline__ void mlp16(const __half *Xs, const NetHalf &N, float 
   uint32_t a2[2][4];
 #pragma unroll
   for (int kt = 0; kt < 2; ++kt) {
-    a2[kt][0] = pack_h2(tanh_fast(h[2 * kt][0]), tanh_fast(h[2 * kt][1]));
-    a2[kt][1] = pack_h2(tanh_fast(h[2 * kt][2]), tanh_fast(h[2 * kt][3]));
-    a2[kt][2] = pack_h2(tanh_fast(h[2 * kt + 1][0]), tanh_fast(h[2 * kt + 1][1]));
-    a2[kt][3] = pack_h2(tanh_fast(h[2 * kt + 1][2]), tanh_fast(h[2 * kt + 1][3]));
+    a2[kt][0] = tanh_h2(h[2 * kt][0], h[2 * kt][1]);
+    a2[kt][1] = tanh_h2(h[2 * kt][2], h[2 * kt][3]);
+    a2[kt][2] = tanh_h2(h[2 * kt + 1][0], h[2 * kt + 1][1]);
+    a2[kt][3] = tanh_h2(h[2 * kt + 1][2], h[2 * kt + 1][3]);
   }
 #pragma unroll
   for (int nt = 0; nt < 4; ++nt) {
@@ -319,10 +403,10 @@ __device__ __forceinline__ void mlp16(const __half *Xs, const NetHalf &N, float 
   }
 #pragma unroll
   for (int kt = 0; kt < 2; ++kt) {
-    a2[kt][0] = pack_h2(tanh_fast(h[2 * kt][0]), tanh_fast(h[2 * kt][1]));
-    a2[kt][1] = pack_h2(tanh_fast(h[2 * kt][2]), tanh_fast(h[2 * kt][3]));
-    a2[kt][2] = pack_h2(tanh_fast(h[2 * kt + 1][0]), tanh_fast(h[2 * kt + 1][1]));
-    a2[kt][3] = pack_h2(tanh_fast(h[2 * kt + 1][2]), tanh_fast(h[2 * kt + 1][3]));
+    a2[kt][0] = tanh_h2(h[2 * kt][0], h[2 * kt][1]);
+    a2[kt][1] = tanh_h2(h[2 * kt][2], h[2 * kt][3]);
+    a2[kt][2] = tanh_h2(h[2 * kt + 1][0], h[2 * kt + 1][1]);
+    a2[kt][3] = tanh_h2(h[2 * kt + 1][2], h[2 * kt + 1][3]);
   }
   float o[4] = {N.b3[2 * t], N.b3[2 * t + 1], N.b3[2 * t], N.b3[2 * t + 1]};
 #pragma unroll
@@ -338,14 +422,21 @@ __device__ __forceinline__ void mlp16(const __half *Xs, const NetHalf &N, float 
 
 constexpr int kInferWarps = 8;
 
-// Fused layer-cell step: gathers every listed cell's inputs from the
-// current and previous fields, evaluates the network and writes the
-// correction (p, q) of the cell.  A warp takes 16 cells: two lanes per cell,
-// one reading time t, the other t-1.
-__global__ void __launch_bounds__(32 * kInferWarps) k_abc_infer(const LayerCell *cells, long ncells, const float2 *cur,
-                                                                 const float2 *prev, Box keep, int L, int sy, int pitch,
-                                                                 const NetHalf *net, float2 *corr) {
+__device__ __forceinline__ float sigmoid(float y) { return 1.0f / (1.0f + __expf(-y)); }
+
+// One-way coefficients of every ghost cell from the current and previous
+// fields: gather, normalisation and the network in one kernel.  A warp
+// takes 16 consecutive cells, 4 rays (rays start at multiples of 4 cells).
+// The 4 ghost cells of a ray (d = L-3 .. L) read the 8 points d = L-7 .. L
+// of its normal line (points past the layer read as zero): lane 8r + q
+// loads point q of ray r at t and t-1 once into shared memory; then two
+// lanes per cell, one for each time, build the cell's stencils from it.
+// k[i] = (k_p, k_q).
+__global__ void __launch_bounds__(32 * kInferWarps) k_abc_infer(const __grid_constant__ Ghost G, const float2 *cur, const float2 *prev, int sy,
+                                                                 int pitch, const float4 *med, const NetHalf *net,
+                                                                 float2 *kout) {
   __shared__ __align__(16) __half Xs[kInferWarps][16 * kXs];
+  __shared__ float4 Ln[kInferWarps][4][8];  // (p, q at t, p, q at t-1) of each ray's line points
   __shared__ NetHalf N;
   for (int i = threadIdx.x; i < (int)(sizeof(NetHalf) / 4); i += blockDim.x)
     reinterpret_cast<uint32_t *>(&N)[i] = reinterpret_cast<const uint32_t *>(net)[i];
@@ -353,21 +444,44 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_abc_infer(const LayerCell 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = lane >> 1, half_t = lane & 1;
   __half *X = Xs[warp];
+  const long ncells = G.off[6];
   const long ntiles = (ncells + 15) / 16;
   for (long tile = blockIdx.x * (long)kInferWarps + warp; tile < ntiles; tile += (long)gridDim.x * kInferWarps) {
+    {
+      const int ray = lane >> 3, q = lane & 7;
+      const long i0 = tile * 16 + 4 * ray;  // the ray's cell d = L-3
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (i0 < ncells) {
+        const int f = face_of(G, i0);
+        const long at = (long)__float_as_int(med[i0].w) + (long)(q - kGhostD) * normal_step(f, sy, pitch);
+        const float2 a = cur[at], b = prev[at];
+        v = make_float4(a.x, a.y, b.x, b.y);
+      }
+      Ln[warp][ray][q] = v;
+    }
+    __syncwarp();
     const long ci = tile * 16 + r;
-    float v[18];
+    float vv[18];
     float s = 0.f;
-    LayerCell lc = {0, 0, 0, 0, 0.f, 0.f, 0.f, 0.f};
+    float4 m = make_float4(0.f, 0.f, 0.f, 0.f);
+    int d = 0;
     if (ci < ncells) {
-      lc = cells[ci];
-      const int a = lc.code & 3, sgn = (lc.code & 4) ? 1 : -1;
-      normal_stencil(half_t ? prev : cur, lc.x, lc.y, lc.z, a, sgn, keep, sy, pitch, v, v + 9);
+      m = med[ci];
+      const int j = r & 3;  // d = L-3 + j: line points j .. j+8 (past 7: zero)
+      d = G.L - kGhostD + 1 + j;
+      const float4 *line = Ln[warp][r >> 2];
 #pragma unroll
-      for (int k = 0; k < 18; ++k) s = fmaxf(s, fabsf(v[k]));
+      for (int o = 0; o < 9; ++o) {
+        const int q = j + o;
+        const float4 u = q < 8 ? line[q < 8 ? q : 7] : make_float4(0.f, 0.f, 0.f, 0.f);
+        vv[o] = half_t ? u.z : u.x;
+        vv[9 + o] = half_t ? u.w : u.y;
+      }
+#pragma unroll
+      for (int k = 0; k < 18; ++k) s = fmaxf(s, fabsf(vv[k]));
     } else {
 #pragma unroll
-      for (int k = 0; k < 18; ++k) v[k] = 0.f;
+      for (int k = 0; k < 18; ++k) vv[k] = 0.f;
     }
     s = fmaxf(s, __shfl_xor_sync(0xffffffffu, s, 1));
     // Stencils this small carry no wave (the first cells a front reaches
@@ -377,12 +491,12 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_abc_infer(const LayerCell 
     __half *row = X + r * kXs + 18 * half_t;
 #pragma unroll
     for (int k = 0; k < 18; k += 2)
-      *reinterpret_cast<__half2 *>(row + k) = __floats2half2_rn(v[k] * inv, v[k + 1] * inv);
+      *reinterpret_cast<__half2 *>(row + k) = __floats2half2_rn(vv[k] * inv, vv[k + 1] * inv);
     if (half_t == 0) {
-      X[r * kXs + 36] = __float2half_rn(lc.vpz * kVScale);
-      X[r * kXs + 37] = __float2half_rn(lc.eps);
-      X[r * kXs + 38] = __float2half_rn(lc.del);
-      X[r * kXs + 39] = __float2half_rn((float)(lc.code >> 3) / (float)L);
+      X[r * kXs + 36] = __float2half_rn(m.x * kVScale);
+      X[r * kXs + 37] = __float2half_rn(m.y);
+      X[r * kXs + 38] = __float2half_rn(m.z);
+      X[r * kXs + 39] = __float2half_rn((float)d / (float)G.L);
     } else {
 #pragma unroll
       for (int k = 40; k < kK1; ++k) X[r * kXs + k] = __float2half_rn(0.f);
@@ -391,12 +505,10 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_abc_infer(const LayerCell 
     float ylo[2], yhi[2];
     mlp16(X, N, ylo, yhi);
     const int g = lane >> 2;
-    const float s_lo = __shfl_sync(0xffffffffu, s, 2 * g), s_hi = __shfl_sync(0xffffffffu, s, 2 * (g + 8));
     if ((lane & 3) == 0) {
       const long c0 = tile * 16 + g, c1 = tile * 16 + g + 8;
-      const float k0 = s_lo * N.out_scale, k1 = s_hi * N.out_scale;
-      if (c0 < ncells) corr[c0] = make_float2(ylo[0] * k0, ylo[1] * k0);
-      if (c1 < ncells) corr[c1] = make_float2(yhi[0] * k1, yhi[1] * k1);
+      if (c0 < ncells) kout[c0] = make_float2(sigmoid(ylo[0]), sigmoid(ylo[1]));
+      if (c1 < ncells) kout[c1] = make_float2(sigmoid(yhi[0]), sigmoid(yhi[1]));
     }
     __syncwarp();
   }
@@ -438,39 +550,108 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_abc_forward(const float *f
   }
 }
 
-// The layer's step after the plain update: next[cell] += corr[cell] for the
-// first nnet listed cells (the network's), then every layer cell is scaled
-// by its taper weight exp(-(damping * d)^2) (1 when damping is 0).
-__global__ void k_abc_add(const LayerCell *cells, long ncells, long nnet, const float2 *corr, float2 *next, int sy,
-                          int pitch, float damping) {
+// The one-way update of the rays of faces f0 and f0 + 1 (one axis), after
+// the plain step: next[g] = cur[i] + k (cur[g] - next[i]) outward from
+// d = L-3.  Four lanes per ray, one per cell (d = L-3 + lane % 4): each
+// loads its cell's coefficient and current value (the inward one comes from
+// the lane before), the lane of d = L-3 also the inward neighbour's current
+// and next values;
+// the outward dependence next_d = A_d - k_d next_(d-1) (A_d = cur_(d-1) +
+// k_d cur_d) is an inclusive scan of affine maps over the 4 lanes (two
+// shuffle rounds).  The rays of one face are independent.
+__global__ void k_abc_rays(const __grid_constant__ Ghost G, int f0, const float2 *__restrict__ cur,
+                           float2 *__restrict__ next, int sy, int pitch, const float2 *__restrict__ k) {
+  const int rays = (int)((G.off[f0 + 1] - G.off[f0]) / kGhostD);
+  const int lane = threadIdx.x & 31, j = lane & 3;
+  // Whole warps step through the rays together (shuffles need every lane).
+  const long nthreads = (long)2 * rays * kGhostD;
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long t0 = (long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); t0 < nthreads; t0 += stride) {
+    const long t = t0 + lane;
+    const bool live = t < nthreads;
+    const int r = (int)(t / kGhostD);
+    const int f = f0 + (r >= rays ? 1 : 0);
+    const int ray = r - (f - f0) * rays;
+    float2 kk = make_float2(0.f, 0.f), cg = make_float2(0.f, 0.f), ci = make_float2(0.f, 0.f), ni = ci;
+    int gidx = 0;
+    if (live) {
+      const int a = face_axis(f);
+      int t0i, t1i;
+      transverse(a, t0i, t1i);
+      const int e0 = G.keep.hi[t0i] - G.keep.lo[t0i];
+      const int d = G.L - kGhostD + 1 + j;
+      int c[3];
+      c[t0i] = G.keep.lo[t0i] + ray % e0;
+      c[t1i] = G.keep.lo[t1i] + ray / e0;
+      c[a] = face_sign(f) < 0 ? G.in.lo[a] - d : G.in.hi[a] - 1 + d;
+      gidx = (int)cell_index(c[0], c[1], c[2], sy, pitch);
+      kk = k[G.off[f] + (long)ray * kGhostD + j];
+      cg = cur[gidx];
+      if (j == 0) {
+        const int step = normal_step(f, sy, pitch);
+        ci = cur[gidx - step];
+        ni = next[gidx - step];
+      }
+    }
+    // The inward cell of lanes 1 .. 3 is the cell of the lane before.
+    {
+      const float ux = __shfl_up_sync(0xffffffffu, cg.x, 1), uy = __shfl_up_sync(0xffffffffu, cg.y, 1);
+      if (j != 0) ci = make_float2(ux, uy);
+    }
+    // a_d = cur_(d-1) + k_d cur_d, next_d = a_d - k_d next_(d-1): lane j
+    // folds in lanes j-1 .. 0 of its ray (the first one brings next_(L-4)).
+    float ax = __fmaf_rn(kk.x, cg.x, ci.x), ay = __fmaf_rn(kk.y, cg.y, ci.y);
+    float mx = -kk.x, my = -kk.y;  // coefficient of next_(start-1) in the running value
+    if (j == 0) {
+      ax = __fmaf_rn(mx, ni.x, ax);
+      ay = __fmaf_rn(my, ni.y, ay);
+      mx = 0.f;
+      my = 0.f;
+    }
+#pragma unroll
+    for (int o = 1; o < kGhostD; o <<= 1) {
+      const float px = __shfl_up_sync(0xffffffffu, ax, o), py = __shfl_up_sync(0xffffffffu, ay, o);
+      const float qx = __shfl_up_sync(0xffffffffu, mx, o), qy = __shfl_up_sync(0xffffffffu, my, o);
+      if (j >= o) {
+        // value = a + m * (previous value) with the previous one = p + q * (...)
+        ax = __fmaf_rn(mx, px, ax);
+        ay = __fmaf_rn(my, py, ay);
+        mx *= qx;
+        my *= qy;
+      }
+    }
+    if (live) next[gidx] = make_float2(ax, ay);
+  }
+}
+
+// Taper of the layer cells after the step: next *= exp(-(damping d)^2).
+__global__ void k_abc_taper(const LayerCell *cells, long ncells, float2 *next, int sy, int pitch, float damping) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ncells; i += (long)gridDim.x * blockDim.x) {
     const LayerCell c = cells[i];
-    float2 *p = next + ((size_t)c.z * sy + c.y) * pitch + c.x;
+    float2 *p = next + cell_index(c.x, c.y, c.z, sy, pitch);
+    const float a = damping * (float)c.d;
+    const float w = __expf(-a * a);
     float2 v = *p;
-    if (i < nnet) {
-      const float2 d = corr[i];
-      v.x += d.x;
-      v.y += d.y;
-    }
-    if (damping > 0.f) {
-      const float a = damping * (float)(c.code >> 3);
-      const float w = __expf(-a * a);
-      v.x *= w;
-      v.y *= w;
-    }
+    v.x *= w;
+    v.y *= w;
     *p = v;
   }
 }
 
-// Medium of the listed cells from the coefficient block.
-__global__ void k_abc_fill_medium(LayerCell *cells, long ncells, const float *coef, int sy, int pitch) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ncells; i += (long)gridDim.x * blockDim.x) {
-    LayerCell c = cells[i];
-    const float4 m = medium_of(coef, c.x, c.y, c.z, sy, pitch);
-    c.vpz = m.x;
-    c.eps = m.y;
-    c.del = m.z;
-    cells[i] = c;
+// Medium of every ghost cell (inputs of the network) with the cell's index
+// in the field in .w (as int bits), and the medium's one-way coefficients.
+__global__ void k_abc_fill(const __grid_constant__ Ghost G, const float *coef, int sy, int pitch, float dt, float hx, float hy, float hz,
+                           float4 *med, float2 *kfix) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < G.off[6]; i += (long)gridDim.x * blockDim.x) {
+    int c[3], f, a, sgn;
+    ghost_cell(G, i, c, f, a, sgn);
+    float4 m = medium_of(coef, c[0], c[1], c[2], sy, pitch);
+    m.w = __int_as_float((int)cell_index(c[0], c[1], c[2], sy, pitch));
+    med[i] = m;
+    if (kfix) {
+      const float kf = oneway_k(m.x, m.y, a, dt, a == 0 ? hx : (a == 1 ? hy : hz));
+      kfix[i] = make_float2(kf, kf);
+    }
   }
 }
 
@@ -482,14 +663,14 @@ constexpr int sX = 41, sH = 33;
 __device__ __forceinline__ float h16(float v) { return __half2float(__float2half_rn(v)); }
 
 // Forward and backward of B samples (index b of the batch: a random sample,
-// or b itself when seed is 0): loss += sum (y - t * tgt_scale)^2 / (2 B),
-// gradients summed into grad.  Weights are used FP16-rounded, activations
-// are rounded to FP16 between layers (as inference does), the derivatives
-// treat both roundings as the identity.  noise > 0 perturbs the stencil
-// inputs.
+// or b itself when seed is 0): loss += sum_c (sigmoid(y_c) a_c - b_c)^2 /
+// (2 B), gradients summed into grad.  Weights are used FP16-rounded,
+// activations are rounded to FP16 between layers (as inference does), the
+// derivatives treat both roundings as the identity.  noise > 0 perturbs the
+// stencil inputs.
 __global__ void __launch_bounds__(kTB) k_abc_train(const float *feat, const float *tgt, long nsamp, int B,
-                                                    uint32_t seed, const float *P, float tgt_scale, float noise,
-                                                    float *grad, float *loss) {
+                                                    uint32_t seed, const float *P, float noise, float *grad,
+                                                    float *loss) {
   extern __shared__ float sm[];
   float *W1 = sm, *b1 = W1 + kHid * kIn, *W2 = b1 + kHid, *b2 = W2 + kHid * kHid, *W3 = b2 + kHid,
         *b3 = W3 + kOut * kHid;
@@ -510,8 +691,7 @@ __global__ void __launch_bounds__(kTB) k_abc_train(const float *feat, const floa
   for (int k = 0; k < kIn; ++k) {
     float f = live ? feat[si * kIn + k] : 0.f;
     if (noise > 0.f && k < kSt && live) {
-      // Input noise (approximately normal, from four uniforms): the network
-      // learns to respond weakly to perturbations of the layer's fields.
+      // Input noise (approximately normal, from four uniforms).
       float u = 0.f;
       for (int r = 0; r < 4; ++r) u += (float)(mix32(seed ^ (0x51ED27u * (r + 1)), (uint32_t)(b * kIn + k)) >> 8);
       f += noise * 1.7320508f * (u * (1.0f / 16777216.0f) - 2.0f);
@@ -537,9 +717,15 @@ __global__ void __launch_bounds__(kTB) k_abc_train(const float *feat, const floa
   for (int o = 0; o < kOut; ++o) {
     float y = b3[o];
     for (int k = 0; k < kHid; ++k) y = fmaf(W3[o * kHid + k], h2[k], y);
-    const float e = live ? y - tgt[si * kOut + o] * tgt_scale : 0.f;
-    l += e * e;
-    dy[o] = e / (float)B;
+    float g = 0.f;
+    if (live) {
+      const float kk = 1.0f / (1.0f + expf(-y));
+      const float ta = tgt[si * kTgt + o], tb = tgt[si * kTgt + 2 + o];
+      const float e = fmaf(kk, ta, -tb);
+      l += e * e;
+      g = e * ta * kk * (1.0f - kk);
+    }
+    dy[o] = g / (float)B;
   }
   for (int k = 0; k < kHid; ++k) {
     float g = 0.f;
@@ -596,7 +782,7 @@ __global__ void k_abc_adam(float *P, float *grad, float *m, float *v, int n, flo
 }
 
 // FP32 master weights -> inference copy.
-__global__ void k_abc_pack(const float *P, float out_scale, NetHalf *N) {
+__global__ void k_abc_pack(const float *P, NetHalf *N) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < kHid * kK1) {
     const int o = i / kK1, k = i % kK1;
@@ -609,15 +795,6 @@ __global__ void k_abc_pack(const float *P, float out_scale, NetHalf *N) {
     N->b2[i] = P[oB2 + i];
   }
   if (i < 8) N->b3[i] = i < kOut ? P[oB3 + i] : 0.f;
-  if (i == 0) N->out_scale = out_scale;
-}
-
-__global__ void k_sumsq(const float *v, long n, double *out) {
-  double s = 0.0;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-    s += (double)v[i] * v[i];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
 }
 
 // ---- host state -------------------------------------------------------------------
@@ -627,23 +804,25 @@ namespace {
 struct Trainer {
   float *P = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;  // master weights and Adam state
   NetHalf *net = nullptr;
-  float out_scale = 1.0f;
   bool weights = false;
   long adam_t = 0;
   float *feat = nullptr, *tgt = nullptr;
-  int4 *pos = nullptr;  // grid cell and distance of every sample
+  int4 *pos = nullptr;  // grid cell, face and distance of every sample
   unsigned long long *count = nullptr;
   long cap = 0;
 };
 
 struct ResidentLayer {
   bool on = false;
-  int L = 0, mode = 0;
+  int mode = 0;
+  int interval = 1;  // learned form: network every `interval` steps
+  long steps = 0;    // steps since SetBoundary
   float damping = 0.f;
-  LayerCell *cells = nullptr;  // network cells first, then the other layer cells; z, y, x order in each
-  long ncells = 0, nnet = 0;
-  float2 *corr = nullptr;
-  Box in, keep;
+  Ghost G;
+  float4 *med = nullptr;       // medium of every ghost cell (one-way modes)
+  float2 *k = nullptr;         // one-way coefficients of every ghost cell
+  LayerCell *cells = nullptr;  // every layer cell (taper), z, y, x order
+  long ncells = 0;
 };
 
 Trainer T;
@@ -681,7 +860,7 @@ int ensure_trainer() {
 }
 
 int pack_net(cudaStream_t s) {
-  k_abc_pack<<<(kHid * kK1 + 255) / 256, 256, 0, s>>>(T.P, T.out_scale, T.net);
+  k_abc_pack<<<(kHid * kK1 + 255) / 256, 256, 0, s>>>(T.P, T.net);
   CKA(cudaGetLastError());
   return FLETCHER_OK;
 }
@@ -707,30 +886,42 @@ int train_attr() {
   return FLETCHER_OK;
 }
 
+bool oneway_mode(int mode) { return mode == FLETCHER_BOUNDARY_LEARNED || mode == FLETCHER_BOUNDARY_ONEWAY; }
+
 }  // namespace
 
 bool abc_active() { return R.on; }
 
 void abc_release_resident() {
+  if (R.med) cudaFree(R.med);
+  if (R.k) cudaFree(R.k);
   if (R.cells) cudaFree(R.cells);
-  if (R.corr) cudaFree(R.corr);
   R = ResidentLayer();
 }
 
+int g_interval = 1;  // FLETCHER_AbcSetInterval
+
 cudaError_t abc_before_step(const ResidentView &v) {
-  if (!R.on || !R.nnet) return cudaSuccess;
-  const int grid = (int)(((R.nnet + 15) / 16 + kInferWarps - 1) / kInferWarps);
-  const int cap = v.num_sms > 0 ? v.num_sms * 8 : 1024;
-  k_abc_infer<<<grid < cap ? grid : cap, 32 * kInferWarps, 0, v.stream>>>(R.cells, R.nnet, v.cur, v.prev, R.keep,
-                                                                          R.L, v.sy, v.pitch, T.net, R.corr);
+  if (!R.on || R.mode != FLETCHER_BOUNDARY_LEARNED) return cudaSuccess;
+  if (R.steps++ % R.interval != 0) return cudaSuccess;  // the last coefficients stay
+  const long ntiles = (R.G.off[6] + 15) / 16;
+  const long grid = (ntiles + kInferWarps - 1) / kInferWarps;
+  const long cap = v.num_sms > 0 ? (long)v.num_sms * 8 : 1024;
+  k_abc_infer<<<(int)(grid < cap ? grid : cap), 32 * kInferWarps, 0, v.stream>>>(R.G, v.cur, v.prev, v.sy, v.pitch,
+                                                                                 R.med, T.net, R.k);
   return cudaGetLastError();
 }
 
 cudaError_t abc_after_step(const ResidentView &v) {
-  if (!R.on || !R.ncells) return cudaSuccess;
-  const long n = R.damping > 0.f ? R.ncells : R.nnet;
-  if (!n) return cudaSuccess;
-  k_abc_add<<<grid_of(n, 256), 256, 0, v.stream>>>(R.cells, n, R.nnet, R.corr, v.next, v.sy, v.pitch, R.damping);
+  if (!R.on) return cudaSuccess;
+  if (oneway_mode(R.mode)) {
+    for (int f0 = 0; f0 < 6; f0 += 2) {  // z faces, y faces, x faces
+      const long threads = 2 * (R.G.off[f0 + 1] - R.G.off[f0]);  // one per ghost cell of the two faces
+      k_abc_rays<<<grid_of(threads, 256), 256, 0, v.stream>>>(R.G, f0, v.cur, v.next, v.sy, v.pitch, R.k);
+    }
+  }
+  if (R.damping > 0.f && R.ncells)
+    k_abc_taper<<<grid_of(R.ncells, 256), 256, 0, v.stream>>>(R.cells, R.ncells, v.next, v.sy, v.pitch, R.damping);
   return cudaGetLastError();
 }
 
@@ -740,14 +931,13 @@ using namespace flt;
 
 // ===== Part 4: learned absorbing boundary =========================================
 
-extern "C" int FLETCHER_AbcSetWeights(const float *params, float out_scale) {
-  if (!params || !(out_scale > 0.f)) return err(FLETCHER_ERR_ARGS, "AbcSetWeights: bad arguments");
+extern "C" int FLETCHER_AbcSetWeights(const float *params) {
+  if (!params) return err(FLETCHER_ERR_ARGS, "AbcSetWeights: bad arguments");
   if (ensure_trainer()) return FLETCHER_GetLastError();
   CKA(cudaMemcpy(T.P, params, kNP * sizeof(float), cudaMemcpyHostToDevice));
   CKA(cudaMemset(T.m, 0, kNP * sizeof(float)));
   CKA(cudaMemset(T.v, 0, kNP * sizeof(float)));
   T.adam_t = 0;
-  T.out_scale = out_scale;
   T.weights = true;
   if (pack_net(nullptr)) return FLETCHER_GetLastError();
   CKA(cudaDeviceSynchronize());
@@ -765,14 +955,15 @@ extern "C" int FLETCHER_AbcInit(unsigned seed) {
   fill(oW1, kHid, kIn);
   fill(oW2, kHid, kHid);
   fill(oW3, kOut, kHid);
-  return FLETCHER_AbcSetWeights(p.data(), 1.0f);
+  for (int o = 0; o < kOut; ++o) p[oB3 + o] = kInitBias;
+  return FLETCHER_AbcSetWeights(p.data());
 }
 
-extern "C" int FLETCHER_AbcGetWeights(float *params, float *out_scale) {
+extern "C" int FLETCHER_AbcGetWeights(float *params) {
   if (!T.weights) return err(FLETCHER_ERR_ARGS, "AbcGetWeights: no network");
+  if (!params) return err(FLETCHER_ERR_ARGS, "AbcGetWeights: bad arguments");
   CKA(cudaDeviceSynchronize());
-  if (params) CKA(cudaMemcpy(params, T.P, kNP * sizeof(float), cudaMemcpyDeviceToHost));
-  if (out_scale) *out_scale = T.out_scale;
+  CKA(cudaMemcpy(params, T.P, kNP * sizeof(float), cudaMemcpyDeviceToHost));
   return FLETCHER_OK;
 }
 
@@ -788,7 +979,7 @@ extern "C" int FLETCHER_AbcReserve(long capacity) {
   T.cap = capacity;
   if (capacity) {
     CKA(cudaMalloc(&T.feat, (size_t)capacity * kIn * sizeof(float)));
-    CKA(cudaMalloc(&T.tgt, (size_t)capacity * kOut * sizeof(float)));
+    CKA(cudaMalloc(&T.tgt, (size_t)capacity * kTgt * sizeof(float)));
     CKA(cudaMalloc(&T.pos, (size_t)capacity * sizeof(int4)));
   }
   return FLETCHER_OK;
@@ -808,21 +999,19 @@ extern "C" int FLETCHER_AbcCollect(const int *interior_lo, const int *interior_h
   if (!T.count || !T.cap) return err(FLETCHER_ERR_ARGS, "AbcCollect: call FLETCHER_AbcReserve first");
   if (!interior_lo || !interior_hi || layer < kRadius + 1)
     return err(FLETCHER_ERR_ARGS, "AbcCollect: bad box or layer");
-  Box in, keep;
+  Box in;
   const int dims[3] = {v.sx, v.sy, v.sz};
   for (int a = 0; a < 3; ++a) {
     in.lo[a] = interior_lo[a];
     in.hi[a] = interior_hi[a];
-    keep.lo[a] = in.lo[a] - layer;
-    keep.hi[a] = in.hi[a] + layer;
-    // The target reads 4 cells beyond the kept box; all of it must be updated grid.
-    if (in.hi[a] <= in.lo[a] || keep.lo[a] - kRadius < v.bord || keep.hi[a] + kRadius > dims[a] - v.bord)
+    // The next values read 4 cells beyond the kept box; all of it must be updated grid.
+    if (in.hi[a] <= in.lo[a] || in.lo[a] - layer - kRadius < v.bord || in.hi[a] + layer + kRadius > dims[a] - v.bord)
       return err(FLETCHER_ERR_ARGS, "AbcCollect: the box and its layer must lie 4 cells inside the updated region");
   }
-  const long n = (long)(keep.hi[0] - keep.lo[0]) * (keep.hi[1] - keep.lo[1]) * (keep.hi[2] - keep.lo[2]);
-  k_abc_collect<<<grid_of(n, 256), 256, 0, v.stream>>>(v.cur, v.prev, v.coef, in, keep, layer, v.sy, v.pitch, v.dx,
-                                                       v.dy, v.dz, v.dt, keep_frac, seed, min_scale, T.feat, T.tgt,
-                                                       T.pos, T.count, (unsigned long long)T.cap);
+  const Ghost G = make_ghost(in, layer);
+  k_abc_collect<<<grid_of(G.off[6], 256), 256, 0, v.stream>>>(v.cur, v.prev, v.coef, G, v.sy, v.pitch, v.dx, v.dy,
+                                                               v.dz, v.dt, keep_frac, seed, min_scale, T.feat, T.tgt,
+                                                               T.pos, T.count, (unsigned long long)T.cap);
   CKA(cudaGetLastError());
   CKA(cudaStreamSynchronize(v.stream));
   return FLETCHER_OK;
@@ -833,7 +1022,7 @@ extern "C" int FLETCHER_AbcGetSamples(long start, long n, float *feat, float *tg
   if (start < 0 || n < 0 || start + n > have)
     return err(FLETCHER_ERR_ARGS, "AbcGetSamples: range outside the samples");
   if (feat) CKA(cudaMemcpy(feat, T.feat + start * kIn, n * kIn * sizeof(float), cudaMemcpyDeviceToHost));
-  if (tgt) CKA(cudaMemcpy(tgt, T.tgt + start * kOut, n * kOut * sizeof(float), cudaMemcpyDeviceToHost));
+  if (tgt) CKA(cudaMemcpy(tgt, T.tgt + start * kTgt, n * kTgt * sizeof(float), cudaMemcpyDeviceToHost));
   if (pos) CKA(cudaMemcpy(pos, T.pos + start, n * sizeof(int4), cudaMemcpyDeviceToHost));
   return FLETCHER_OK;
 }
@@ -846,20 +1035,6 @@ extern "C" int FLETCHER_AbcTrain(int iters, int batch, float lr, unsigned seed, 
     return err(FLETCHER_ERR_ARGS, "AbcTrain: bad arguments");
   cudaStream_t s = stream_of();
   if (train_attr()) return FLETCHER_GetLastError();
-  // Output scale: the root mean square of the targets, fixed at the first
-  // training of these weights (Adam's state restarts with it).
-  if (T.adam_t == 0) {
-    double *d = nullptr;
-    CKA(cudaMalloc(&d, sizeof(double)));
-    CKA(cudaMemsetAsync(d, 0, sizeof(double), s));
-    k_sumsq<<<1024, 256, 0, s>>>(T.tgt, ns * kOut, d);
-    double sq = 0.0;
-    CKA(cudaMemcpyAsync(&sq, d, sizeof(double), cudaMemcpyDeviceToHost, s));
-    CKA(cudaStreamSynchronize(s));
-    cudaFree(d);
-    const double rms = sqrt(sq / (double)(ns * kOut));
-    T.out_scale = rms > 0.0 ? (float)rms : 1.0f;
-  }
   float *loss = nullptr;
   CKA(cudaMalloc(&loss, iters * sizeof(float)));
   CKA(cudaMemsetAsync(loss, 0, iters * sizeof(float), s));
@@ -869,8 +1044,7 @@ extern "C" int FLETCHER_AbcTrain(int iters, int batch, float lr, unsigned seed, 
   for (int it = 0; it < iters; ++it) {
     uint64_t st = (uint64_t)seed * 1000003ull + (uint64_t)it;
     const uint32_t sd = (uint32_t)splitmix(st) | 1u;
-    k_abc_train<<<blocks, kTB, kTrainSmem, s>>>(T.feat, T.tgt, ns, batch, sd, T.P, 1.0f / T.out_scale, noise,
-                                                T.grad, loss + it);
+    k_abc_train<<<blocks, kTB, kTrainSmem, s>>>(T.feat, T.tgt, ns, batch, sd, T.P, noise, T.grad, loss + it);
     ++T.adam_t;
     const float lr_t = lr * 0.5f * (1.0f + cosf(3.14159265f * (float)it / (float)iters));
     k_abc_adam<<<(kNP + 255) / 256, 256, 0, s>>>(T.P, T.grad, T.m, T.v, kNP, lr_t, b1, b2, 1e-8f,
@@ -890,14 +1064,14 @@ extern "C" int FLETCHER_AbcGradient(const float *feat, const float *tgt, int n, 
   if (train_attr()) return FLETCHER_GetLastError();
   float *df = nullptr, *dt = nullptr, *dl = nullptr, *dg = nullptr;
   CKA(cudaMalloc(&df, (size_t)n * kIn * sizeof(float)));
-  CKA(cudaMalloc(&dt, (size_t)n * kOut * sizeof(float)));
+  CKA(cudaMalloc(&dt, (size_t)n * kTgt * sizeof(float)));
   CKA(cudaMalloc(&dl, sizeof(float)));
   CKA(cudaMalloc(&dg, kNP * sizeof(float)));
   CKA(cudaMemcpy(df, feat, (size_t)n * kIn * sizeof(float), cudaMemcpyHostToDevice));
-  CKA(cudaMemcpy(dt, tgt, (size_t)n * kOut * sizeof(float), cudaMemcpyHostToDevice));
+  CKA(cudaMemcpy(dt, tgt, (size_t)n * kTgt * sizeof(float), cudaMemcpyHostToDevice));
   CKA(cudaMemset(dl, 0, sizeof(float)));
   CKA(cudaMemset(dg, 0, kNP * sizeof(float)));
-  k_abc_train<<<(n + kTB - 1) / kTB, kTB, kTrainSmem>>>(df, dt, n, n, 0u, T.P, 1.0f, 0.f, dg, dl);
+  k_abc_train<<<(n + kTB - 1) / kTB, kTB, kTrainSmem>>>(df, dt, n, n, 0u, T.P, 0.f, dg, dl);
   CKA(cudaGetLastError());
   CKA(cudaMemcpy(grad, dg, kNP * sizeof(float), cudaMemcpyDeviceToHost));
   if (loss) CKA(cudaMemcpy(loss, dl, sizeof(float), cudaMemcpyDeviceToHost));
@@ -929,12 +1103,12 @@ extern "C" int FLETCHER_SetBoundary(int mode, int layer, float damping) {
   if (!v.init) return err(FLETCHER_ERR_ARGS, "SetBoundary needs an initialised FP32 resident state");
   abc_release_resident();
   if (mode == FLETCHER_BOUNDARY_PLAIN) return FLETCHER_OK;
-  if (mode != FLETCHER_BOUNDARY_LEARNED && mode != FLETCHER_BOUNDARY_SPONGE)
+  if (mode != FLETCHER_BOUNDARY_LEARNED && mode != FLETCHER_BOUNDARY_SPONGE && mode != FLETCHER_BOUNDARY_ONEWAY)
     return err(FLETCHER_ERR_ARGS, "SetBoundary: unknown mode");
-  const bool net = mode == FLETCHER_BOUNDARY_LEARNED;
-  if (net && !T.weights) return err(FLETCHER_ERR_ARGS, "SetBoundary: the learned layer needs weights");
+  if (mode == FLETCHER_BOUNDARY_LEARNED && !T.weights)
+    return err(FLETCHER_ERR_ARGS, "SetBoundary: the learned layer needs weights");
   if (layer < kRadius + 1) return err(FLETCHER_ERR_ARGS, "SetBoundary: layer must be at least 5 cells");
-  if (!(damping >= 0.f) || (!net && !(damping > 0.f)))
+  if (!(damping >= 0.f) || (mode == FLETCHER_BOUNDARY_SPONGE && !(damping > 0.f)))
     return err(FLETCHER_ERR_ARGS, "SetBoundary: damping must be >= 0 (> 0 for the sponge)");
   const int dims[3] = {v.sx, v.sy, v.sz};
   Box in, keep;
@@ -945,39 +1119,56 @@ extern "C" int FLETCHER_SetBoundary(int mode, int layer, float damping) {
     in.hi[a] = dims[a] - v.bord - layer;
     if (in.hi[a] <= in.lo[a]) return err(FLETCHER_ERR_ARGS, "SetBoundary: no interior inside the layer");
   }
-  // Layer cells in z, y, x order (coalesced gathers): the network's first.
-  std::vector<LayerCell> cells[2];
-  for (int z = keep.lo[2]; z < keep.hi[2]; ++z)
-    for (int y = keep.lo[1]; y < keep.hi[1]; ++y) {
-      const bool inner = z >= in.lo[2] && z < in.hi[2] && y >= in.lo[1] && y < in.hi[1];
-      for (int x = keep.lo[0]; x < keep.hi[0]; x = (inner && x == in.lo[0]) ? in.hi[0] : x + 1) {
-        if (inner && x >= in.lo[0] && x < in.hi[0]) continue;
-        int ax, sg;
-        const int d = outside_of(in, x, y, z, &ax, &sg);
-        if (d == 0) continue;
-        LayerCell lc = {x, y, z, ax | (sg > 0 ? 4 : 0) | (d << 3), 0.f, 0.f, 0.f, 0.f};
-        cells[(net && d > layer - kRadius && far_axes(in, x, y, z, layer) == 1) ? 0 : 1].push_back(lc);
+  R.G = make_ghost(in, layer);
+  if ((long)v.sz * v.sy * v.pitch >= (1l << 31))
+    return err(FLETCHER_ERR_ARGS, "SetBoundary: the layer needs a field of fewer than 2^31 cells");
+  if (oneway_mode(mode)) {
+    const long n = R.G.off[6];
+    CKA(cudaMalloc(&R.med, n * sizeof(float4)));
+    CKA(cudaMalloc(&R.k, n * sizeof(float2)));
+    k_abc_fill<<<grid_of(n, 256), 256, 0, v.stream>>>(R.G, v.coef, v.sy, v.pitch, v.dt, v.dx, v.dy, v.dz, R.med,
+                                                      R.k);
+    CKA(cudaGetLastError());
+  }
+  if (damping > 0.f) {
+    // Layer cells in z, y, x order (coalesced).
+    std::vector<LayerCell> cells;
+    for (int z = keep.lo[2]; z < keep.hi[2]; ++z)
+      for (int y = keep.lo[1]; y < keep.hi[1]; ++y) {
+        const bool inner = z >= in.lo[2] && z < in.hi[2] && y >= in.lo[1] && y < in.hi[1];
+        for (int x = keep.lo[0]; x < keep.hi[0]; x = (inner && x == in.lo[0]) ? in.hi[0] : x + 1) {
+          if (inner && x >= in.lo[0] && x < in.hi[0]) continue;
+          const int c[3] = {x, y, z};
+          int d = 0;
+          for (int a = 0; a < 3; ++a) {
+            const int lo = in.lo[a] - c[a], hi = c[a] - (in.hi[a] - 1);
+            d = lo > d ? lo : d;
+            d = hi > d ? hi : d;
+          }
+          if (d > 0) cells.push_back({x, y, z, d});
+        }
       }
-    }
-  R.nnet = (long)cells[0].size();
-  R.ncells = R.nnet + (long)cells[1].size();
-  cells[0].insert(cells[0].end(), cells[1].begin(), cells[1].end());
-  CKA(cudaMalloc(&R.cells, R.ncells * sizeof(LayerCell)));
-  CKA(cudaMalloc(&R.corr, (R.nnet ? R.nnet : 1) * sizeof(float2)));
-  CKA(cudaMemcpyAsync(R.cells, cells[0].data(), R.ncells * sizeof(LayerCell), cudaMemcpyHostToDevice, v.stream));
-  k_abc_fill_medium<<<grid_of(R.ncells, 256), 256, 0, v.stream>>>(R.cells, R.ncells, v.coef, v.sy, v.pitch);
-  CKA(cudaGetLastError());
+    R.ncells = (long)cells.size();
+    CKA(cudaMalloc(&R.cells, R.ncells * sizeof(LayerCell)));
+    CKA(cudaMemcpyAsync(R.cells, cells.data(), R.ncells * sizeof(LayerCell), cudaMemcpyHostToDevice, v.stream));
+  }
   CKA(cudaStreamSynchronize(v.stream));
-  R.in = in;
-  R.keep = keep;
-  R.L = layer;
   R.mode = mode;
   R.damping = damping;
+  R.interval = g_interval;
+  R.steps = 0;
   R.on = true;
   return FLETCHER_OK;
 }
 
-extern "C" long FLETCHER_AbcLayerCells(void) { return R.on ? R.nnet : 0; }
+extern "C" int FLETCHER_AbcSetInterval(int steps) {
+  if (steps < 1) return err(FLETCHER_ERR_ARGS, "AbcSetInterval: steps must be >= 1");
+  g_interval = steps;
+  if (R.on) R.interval = steps;
+  return FLETCHER_OK;
+}
+
+extern "C" long FLETCHER_AbcLayerCells(void) { return (R.on && oneway_mode(R.mode)) ? R.G.off[6] : 0; }
 
 extern "C" void FLETCHER_AbcRelease(void) {
   abc_release_resident();

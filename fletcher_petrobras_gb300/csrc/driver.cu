@@ -19,6 +19,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "../../include/fletcher_gb300.h"
@@ -50,7 +51,9 @@ struct State {
   ShotDesc desc;                 // the shot (passed by value to every launch)
   ShotMaps maps;                 // its TMA descriptors
   int tile_rows = 12, stages = 5, zchunks = 0;
-  int grid = 0, nitems = 0, ntx = 0, nty = 0, nchunk = 0, chunk = 0;
+  int grid = 0, nitems = 0, ntx = 0, nty = 0;
+  int4 *seg = nullptr;     // single-shot work segments {x0, y0, z0, z1}
+  int *cta_first = nullptr;  // [grid + 1]: first segment of each CTA
   long launches = 0;
   size_t dev_bytes = 0;
   int num_sms = 0;
@@ -271,27 +274,95 @@ int grid_for(size_t n) {
 
 // Chooses the number of z-chunks: balances the persistent CTAs' last round
 // against the 8 warm-up planes each chunk re-reads.
-void choose_chunks(int ctas, int tiles, int depth, int req, int *nchunk, int *chunk) {
-  if (req > 0) {
-    *nchunk = req < depth ? req : depth;
-  } else {
-    double best = -1.0;
-    int bc = 1;
-    for (int c = 1; c <= 16 && c <= depth; ++c) {
-      const int len = (depth + c - 1) / c;
-      const int cc = (depth + len - 1) / len;
-      const double items = (double)tiles * cc;
-      const double rounds = ceil(items / ctas);
-      const double eff = (items / ctas) / rounds * (double)len / (len + 4.0);
-      if (eff > best + 1e-9) {
-        best = eff;
-        bc = c;
+// Work split of one shot among `ctas` persistent CTAs, as segments {x0, y0,
+// z0, z1} (a z range of one tile column) listed CTA by CTA.  The tiles
+// (x fastest) are cut into z-chunks; the chunk-major items fill whole rounds
+// of `ctas` (CTA b takes items b, b + ctas, ...: CTAs side by side work on
+// neighbouring tiles at the same depth and share their halo rows through
+// L2).  With `spread`, each item of the last, partial round is then cut into
+// equal z pieces of at least kMinPiece planes, as many as lets every CTA
+// take at most one piece; without it the partial round stays round-robin.
+// The plan (chunk count 1..16 or `req`, spread or not) minimises the busiest
+// CTA's cost: its planes plus kHaloCost a segment for the 8 halo planes,
+// shared-out pieces counting 3/2 (measured on GB300 at 280^3, 328^3 and
+// 576^3: the pieces of neighbouring tiles run at different depths and lose
+// their L2 halo sharing); a spread plan must beat the best round-robin one
+// by 3%.
+constexpr int kMinPiece = 8;
+constexpr int kHaloCost = 4;
+
+struct Split {
+  std::vector<int4> seg;
+  std::vector<int> first;
+  long max_cost = 0, total_cost = 0;
+};
+
+Split split_work(int ctas, int ntx, int nty, int TY, int zlo, int depth, int nchunk, bool spread = true) {
+  const int ntiles = ntx * nty;
+  const int len = (depth + nchunk - 1) / nchunk;
+  const int cc = (depth + len - 1) / len;
+  const long items = (long)ntiles * cc;
+  const long full = spread ? items / ctas * ctas : items;
+  auto tile_x0 = [&](long t) { return kRadius + (int)(t % ntx) * kTileX; };
+  auto tile_y0 = [&](long t) { return kRadius + (int)(t / ntx) * TY; };
+  auto item_z = [&](long i, int *z0, int *z1) {
+    const int ch = (int)(i / ntiles);
+    *z0 = ch * len;
+    *z1 = std::min(depth, *z0 + len);
+  };
+  std::vector<std::vector<int4>> per(ctas);
+  std::vector<long> cost(ctas, 0);
+  for (long i = 0; i < full; ++i) {
+    int z0, z1;
+    item_z(i, &z0, &z1);
+    const long t = i % ntiles;
+    per[i % ctas].push_back(make_int4(tile_x0(t), tile_y0(t), zlo + z0, zlo + z1));
+    cost[i % ctas] += 2 * ((z1 - z0) + kHaloCost);  // costs in half planes
+  }
+  // The partial round: each of its items cut into p equal z pieces (at
+  // least kMinPiece planes, p * items <= ctas), one piece per CTA.
+  const long rem = items - full;
+  if (rem > 0) {
+    const long p = std::max(1L, std::min((long)ctas / rem, (long)len / kMinPiece));
+    long b = 0;
+    for (long i = full; i < items; ++i) {
+      int z0, z1;
+      item_z(i, &z0, &z1);
+      const long t = i % ntiles, n = z1 - z0;
+      for (long j = 0; j < p; ++j, ++b) {
+        const int a0 = z0 + (int)(n * j / p), a1 = z0 + (int)(n * (j + 1) / p);
+        if (a1 <= a0) continue;
+        per[b % ctas].push_back(make_int4(tile_x0(t), tile_y0(t), zlo + a0, zlo + a1));
+        cost[b % ctas] += 3 * ((a1 - a0) + kHaloCost);
       }
     }
-    *nchunk = bc;
   }
-  *chunk = (depth + *nchunk - 1) / *nchunk;
-  *nchunk = (depth + *chunk - 1) / *chunk;
+  Split sp;
+  sp.first.push_back(0);
+  for (int b = 0; b < ctas; ++b) {
+    sp.seg.insert(sp.seg.end(), per[b].begin(), per[b].end());
+    sp.first.push_back((int)sp.seg.size());
+    sp.max_cost = std::max(sp.max_cost, cost[b] / 2);
+    sp.total_cost += cost[b] / 2;
+  }
+  return sp;
+}
+
+Split plan_segments(int ctas, int ntx, int nty, int TY, int zlo, int depth, int req) {
+  if (req > 0) return split_work(ctas, ntx, nty, TY, zlo, depth, std::min(req, depth));
+  if (req < 0) return split_work(ctas, ntx, nty, TY, zlo, depth, std::min(-req, depth), false);
+  Split best[2];  // round-robin, spread
+  for (int c = 1; c <= 16 && c <= depth; ++c)
+    for (int spread = 0; spread < 2; ++spread) {
+      Split sp = split_work(ctas, ntx, nty, TY, zlo, depth, c, spread != 0);
+      Split &b = best[spread];
+      if (b.first.empty() || sp.max_cost < b.max_cost || (sp.max_cost == b.max_cost && sp.total_cost < b.total_cost))
+        b = std::move(sp);
+    }
+  // Round-robin keeps neighbouring tiles in step for L2 and measured faster
+  // at 504^3 than a spread plan the model rates 1% cheaper: spread only when
+  // it saves more than 3%.
+  return best[1].max_cost * 100 < best[0].max_cost * 97 ? best[1] : best[0];
 }
 
 int check_dims(int sx, int sy, int sz) {
@@ -336,6 +407,8 @@ void free_state() {
   }
   if (g.E) cudaFree(g.E);
   if (g.Mx) cudaFree(g.Mx);
+  if (g.seg) cudaFree(g.seg);
+  if (g.cta_first) cudaFree(g.cta_first);
   if (g.err_host) cudaFreeHost(g.err_host);
   g = State();
 }
@@ -425,14 +498,25 @@ int setup_tiles(int rows, int stages) {
   g.ntx = (sx - bord - kRadius + kTileX - 1) / kTileX;
   g.nty = (sy - bord - kRadius + TY - 1) / TY;
   const int ctas = g.num_sms * propagate_fp32_ctas_per_sm(TY);
-  choose_chunks(ctas, g.ntx * g.nty, sz - 2 * bord, g.zchunks, &g.nchunk, &g.chunk);
-  g.nitems = g.ntx * g.nty * g.nchunk;
-  g.grid = g.nitems < ctas ? g.nitems : ctas;
+  const Split sp = plan_segments(ctas, g.ntx, g.nty, TY, bord, sz - 2 * bord, g.zchunks);
+  if (g.seg) cudaFree(g.seg);
+  if (g.cta_first) cudaFree(g.cta_first);
+  g.seg = nullptr;
+  g.cta_first = nullptr;
+  CK(cudaMalloc(&g.seg, sp.seg.size() * sizeof(int4)));
+  CK(cudaMalloc(&g.cta_first, sp.first.size() * sizeof(int)));
+  CK(cudaMemcpy(g.seg, sp.seg.data(), sp.seg.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(g.cta_first, sp.first.data(), sp.first.size() * sizeof(int), cudaMemcpyHostToDevice));
+  g.nitems = (int)sp.seg.size();
+  // CTAs past the last one with work are not launched.
+  int grid = ctas;
+  while (grid > 1 && sp.first[grid - 1] == sp.first[grid]) --grid;
+  g.grid = grid;
   memset(&g.desc, 0, sizeof(g.desc));
   g.desc.F[0] = g.F[0];
   g.desc.F[1] = g.F[1];
   g.desc.sx = sx; g.desc.sy = sy; g.desc.sz = sz; g.desc.pitch = g.pitch; g.desc.bord = bord;
-  g.desc.ntx = g.ntx; g.desc.nty = g.nty; g.desc.chunk = g.chunk;
+  g.desc.ntx = g.ntx; g.desc.nty = g.nty;
   g.desc.src_x = g.desc.src_y = g.desc.src_z = -1000;
   g.desc.cor_x = g.desc.cor_y = g.desc.cor_z = -1000;
   return FLETCHER_OK;
@@ -627,6 +711,8 @@ int step() {
   P.shots = nullptr;
   P.maps = nullptr;
   P.items = nullptr;
+  P.seg = g.seg;
+  P.cta_first = g.cta_first;
   P.nitems = g.nitems;
   P.parity = c;
   P.inv_dx = 1.0f / g.dx;
@@ -864,11 +950,22 @@ extern "C" int FLETCHER_SetForm(int form) {
   return FLETCHER_OK;
 }
 
+extern "C" int FLETCHER_PlanSegments(int ctas, int ntx, int nty, int tile_rows, int zlo, int depth, int zchunks,
+                                     int *seg_out, int cap, int *first_out, long *max_cost) {
+  if (ctas < 1 || ntx < 1 || nty < 1 || tile_rows < 1 || depth < 1 || cap < 0 || !first_out)
+    return -fail(FLETCHER_ERR_ARGS, "FLETCHER_PlanSegments: bad arguments");
+  const Split sp = plan_segments(ctas, ntx, nty, tile_rows, zlo, depth, zchunks);
+  const int n = (int)sp.seg.size();
+  if (seg_out && n <= cap) memcpy(seg_out, sp.seg.data(), sizeof(int4) * n);
+  memcpy(first_out, sp.first.data(), sizeof(int) * (ctas + 1));
+  if (max_cost) *max_cost = sp.max_cost;
+  return n;
+}
+
 extern "C" int FLETCHER_SetTileConfig(int rows, int stages, int zchunks) {
   const int r = rows ? rows : 16, s = stages ? stages : 5;
   if (!propagate_fp32_supported(r, s) && !propagate_half_supported(r, s))
     return fail(FLETCHER_ERR_ARGS, "tile shape (%d, %d) is not built", r, s);
-  if (zchunks < 0) return fail(FLETCHER_ERR_ARGS, "zchunks must be >= 0");
   g_req_rows = rows;
   g_req_stages = stages;
   g_req_chunks = zchunks;

@@ -40,13 +40,18 @@ struct alignas(64) ShotMaps {
   CUtensorMap upd;      // coefficients, box (TX, TY, 7, 1)
 };
 
-// One launch: every active shot advances one step.  Work items are
-// {shot, x0, y0, chunk index}, ordered by shot.
+// One launch: every active shot advances one step.
+//  * batched launches: work items {shot, x0, y0, chunk index}, ordered by
+//    shot; CTA b takes items b, b + grid, ... below nitems;
+//  * single-shot launches: segments {x0, y0, z0, z1} (a z range of one tile
+//    column); CTA b takes segments cta_first[b] .. cta_first[b + 1] - 1.
 struct PropParams {
   ShotDesc one;                     // single-shot launches: the shot itself
   const ShotDesc *shots;            // batched launches: per-shot descriptors
   const ShotMaps *maps;
-  const int4 *items;
+  const int4 *items;                // batched launches
+  const int4 *seg;                  // single-shot launches
+  const int *cta_first;             // single-shot launches: [grid + 1]
   int nitems;
   int parity;                       // current field = F[parity], previous = F[1 - parity]
   float inv_dx, inv_dy, inv_dz;     // 1/dx, 1/dy, 1/dz

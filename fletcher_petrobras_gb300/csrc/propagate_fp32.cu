@@ -82,18 +82,24 @@ __device__ __forceinline__ Item decode_item(int item, const PropParams &P) {
     it.z1 = min(it.z0 + d.chunk, d.sz - d.bord);
     it.shot = w.x;
   } else {
-    const ShotDesc &d = P.one;
-    const int tx = item % d.ntx;
-    const int r = item / d.ntx;
-    const int ty = r % d.nty;
-    const int ch = r / d.nty;
-    it.x0 = kRadius + tx * kTileX;
-    it.y0 = kRadius + ty * TY;
-    it.z0 = d.bord + ch * d.chunk;
-    it.z1 = min(it.z0 + d.chunk, d.sz - d.bord);
+    const int4 w = P.seg[item];  // {x0, y0, z0, z1}
+    it.x0 = w.x;
+    it.y0 = w.y;
+    it.z0 = w.z;
+    it.z1 = w.w;
     it.shot = 0;
   }
   return it;
+}
+
+// The items of this CTA: first, end and stride.
+struct ItemRange {
+  int first, end, step;
+};
+template <bool BATCH>
+__device__ __forceinline__ ItemRange item_range(const PropParams &P) {
+  if constexpr (BATCH) return {(int)blockIdx.x, P.nitems, (int)gridDim.x};
+  else return {P.cta_first[blockIdx.x], P.cta_first[blockIdx.x + 1], 1};
 }
 
 // Descriptors used for one step of item `it`.
@@ -125,24 +131,6 @@ __device__ __forceinline__ void issue_step(unsigned char *stage, uint64_t *bar, 
   }
 }
 
-// The step `ahead` steps after step k of `item` in this CTA's sequence.
-template <int TY, bool BATCH>
-__device__ __forceinline__ bool step_after(const PropParams &P, int item, int k, int ahead, Item &out_it,
-                                           int &out_k) {
-  Item it = decode_item<TY, BATCH>(item, P);
-  int kk = k + ahead;
-  while (kk >= it.z1 + kRadius) {
-    const int over = kk - (it.z1 + kRadius);
-    item += gridDim.x;
-    if (item >= P.nitems) return false;
-    it = decode_item<TY, BATCH>(item, P);
-    kk = it.z0 - kRadius + over;
-  }
-  out_it = it;
-  out_k = kk;
-  return true;
-}
-
 template <int TY, int S, bool ISO, bool BATCH, int MINB>
 __global__ void __launch_bounds__(kTileX *TY, MINB)
     k_propagate_fp32(const __grid_constant__ SingleMaps SM, const __grid_constant__ PropParams P) {
@@ -161,7 +149,8 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   const int lx = tid & 31;
   const int ly = tid >> 5;
 
-  if (blockIdx.x >= P.nitems) return;
+  const ItemRange R = item_range<BATCH>(P);
+  if (R.first >= R.end) return;
   // The producer is lane 0 of the last warp (warps 0 .. TY/4-1 carry the
   // halo-column work).  Its cursor, in shared memory, is the next step to load.
   const bool producer = tid == (TY - 1) * 32;
@@ -188,8 +177,8 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
     issue_step<TY>(smem + c.stage * G::STAGE_B, &full[c.stage], c.it, c.k, maps_of(c.it));
     if (++c.stage == S) c.stage = 0;
     if (++c.k >= c.it.z1 + kRadius) {
-      c.item += gridDim.x;
-      if (c.item < P.nitems) {
+      c.item += R.step;
+      if (c.item < R.end) {
         c.it = decode_item<TY, BATCH>(c.item, P);
         c.k = c.it.z0 - kRadius;
       }
@@ -204,8 +193,8 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   }
   if (producer) {
     Cursor c;
-    c.it = decode_item<TY, BATCH>(blockIdx.x, P);
-    c.item = blockIdx.x;
+    c.it = decode_item<TY, BATCH>(R.first, P);
+    c.item = R.first;
     c.k = c.it.z0 - kRadius;
     c.stage = 0;
     *cur = c;
@@ -220,7 +209,7 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
       tma_prefetch_desc(m.upd);
     }
     // Prologue: the first S-2 steps of this CTA.
-    for (int a = 0; a < S - 2 && cur->item < P.nitems; ++a) produce();
+    for (int a = 0; a < S - 2 && cur->item < R.end; ++a) produce();
   }
 
   // Spacing factors (unused on isotropic grids).
@@ -237,7 +226,7 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   uint32_t phase = 0, xphase = 0;
   int dsel = 0;
   int abw = 0;  // shared A/B ring slot of the arriving plane (the plane 4 back is at abw + 1)
-  for (int item = blockIdx.x; item < P.nitems; item += gridDim.x) {
+  for (int item = R.first; item < R.end; item += R.step) {
     const Item it = decode_item<TY, BATCH>(item, P);
     const ShotDesc &sd = BATCH ? P.shots[it.shot] : P.one;
     const int kbeg = it.z0 - kRadius;
@@ -326,7 +315,7 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
         // The producer has passed the exchange of the previous step, so every
         // thread is past the step before it: refill that step's stage with
         // the next step due (S-2 steps ahead of this one).
-        if (producer && cur->item < P.nitems) {
+        if (producer && cur->item < R.end) {
           fence_proxy_async_smem();
           produce();
         }

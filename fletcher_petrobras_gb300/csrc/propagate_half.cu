@@ -115,16 +115,14 @@ struct HItem {
   int x0, y0, z0, z1;
 };
 
-__device__ __forceinline__ HItem decode_hitem(int item, const ShotDesc &d, int TY) {
+// Segment `item` of the launch's list: {x0, y0, z0, z1}.
+__device__ __forceinline__ HItem decode_hitem(int item, const PropParams &P) {
+  const int4 w = P.seg[item];
   HItem it;
-  const int tx = item % d.ntx;
-  const int r = item / d.ntx;
-  const int ty = r % d.nty;
-  const int ch = r / d.nty;
-  it.x0 = kRadius + tx * kTileX;
-  it.y0 = kRadius + ty * TY;
-  it.z0 = d.bord + ch * d.chunk;
-  it.z1 = min(it.z0 + d.chunk, d.sz - d.bord);
+  it.x0 = w.x;
+  it.y0 = w.y;
+  it.z0 = w.z;
+  it.z1 = w.w;
   return it;
 }
 
@@ -173,16 +171,18 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
   const int tid = threadIdx.x;
   const int lx = tid & 31;
   const int ly = tid >> 5;
-  if (blockIdx.x >= P.nitems) return;
+  // This CTA's segments: cta_first[b] .. cta_first[b + 1] - 1.
+  const int item_first = P.cta_first[blockIdx.x], item_end = P.cta_first[blockIdx.x + 1];
+  if (item_first >= item_end) return;
   const bool producer = tid == (TY - 1) * 32;
   auto produce = [&]() {
     int item = cur[0], k = cur[1], stg = cur[2];
-    const HItem it = decode_hitem(item, sd, TY);
+    const HItem it = decode_hitem(item, P);
     issue_half<TY, EXT>(smem + stg * G::STAGE_B, &full[stg], it, k, M);
     if (++stg == S) stg = 0;
     if (++k >= it.z1 + kRadius) {
-      item += gridDim.x;
-      if (item < P.nitems) k = decode_hitem(item, sd, TY).z0 - kRadius;
+      ++item;
+      if (item < item_end) k = decode_hitem(item, P).z0 - kRadius;
     }
     cur[0] = item;
     cur[1] = k;
@@ -192,8 +192,8 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
     for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
     mbar_init(xchg, TY);
     mbar_fence_init();
-    cur[0] = blockIdx.x;
-    cur[1] = decode_hitem(blockIdx.x, sd, TY).z0 - kRadius;
+    cur[0] = item_first;
+    cur[1] = decode_hitem(item_first, P).z0 - kRadius;
     cur[2] = 0;
     smax[0] = smax[1] = 0u;
   }
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
     tma_prefetch_desc(&M.upd);
     // Prologue: S-1 steps; afterwards each step refills the stage freed by
     // the step before it.
-    for (int a = 0; a < S - 1 && cur[0] < P.nitems; ++a) produce();
+    for (int a = 0; a < S - 1 && cur[0] < item_end; ++a) produce();
   }
 
   const float sx1 = P.inv_dx, sy1 = P.inv_dy, sz1 = P.inv_dz;
@@ -222,8 +222,8 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
   int abw = 0;  // shared A/B ring slot of the arriving plane (the plane 4 back is at abw + 1)
   int pend_z = -1;  // thread 0: plane whose CTA maximum waits in smax[sel ^ 1]
   bool bad = false;
-  for (int item = blockIdx.x; item < P.nitems; item += gridDim.x) {
-    const HItem it = decode_hitem(item, sd, TY);
+  for (int item = item_first; item < item_end; ++item) {
+    const HItem it = decode_hitem(item, P);
     const int kbeg = it.z0 - kRadius;
     const int kend = it.z1 + kRadius;
     const int gx = it.x0 + lx;
@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
         // CTA maximum of the plane it updated is complete.  Every thread
         // takes the same branch (a wait that gave up anywhere ends the CTA).
         if (__syncthreads_or(bad)) goto aborted;
-        if (producer && cur[0] < P.nitems) {
+        if (producer && cur[0] < item_end) {
           fence_proxy_async_smem();
           produce();
         }

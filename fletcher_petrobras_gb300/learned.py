@@ -10,11 +10,14 @@ C1 generator, 15 Hz Ricker 8 cells below the interior's top, at its centre):
   comes back from the grid's edge within the run -- the reflection-free
   reference;
 * ``random``: the reference's 32-cell random-velocity shell;
-* ``learned``: an 8-cell layer of extended medium whose outer face cells get
-  the network's correction (every layer cell then scaled by exp(-(a d)^2)
-  when a damping a > 0 is given);
-* ``sponge``: the same layer and scaling without the network;
-* ``plain8``: the same 8-cell layer without either (a zero edge).
+* ``learned``: an 8-cell layer of extended medium whose outer 4 cells get
+  the one-way (box-scheme) update with the network's coefficients
+  (``learned@N``: the network every N steps, the coefficients kept in
+  between);
+* ``oneway``: the same update with the medium's normal-incidence
+  coefficients (the method without the network);
+* ``sponge``: the same layer scaled by exp(-(a d)^2) after every step;
+* ``plain8``: the same 8-cell layer with none of these (a zero edge).
 
 Reflected energy of a form = sum over snapshot times of ||p - p_wide||^2
 over the interior, divided by the same sum of ||p_wide||^2.
@@ -34,7 +37,7 @@ from .models import Problem
 LAYER = 8
 RANDOM_ABSORB = 32
 N_PARAMS = 2434
-BOUNDARY_PLAIN, BOUNDARY_LEARNED, BOUNDARY_SPONGE = 0, 1, 2
+BOUNDARY_PLAIN, BOUNDARY_LEARNED, BOUNDARY_SPONGE, BOUNDARY_ONEWAY = 0, 1, 2, 3
 DAMPING = 0.0
 
 
@@ -89,12 +92,13 @@ def collect(models: int = 64, n_virtual: int = 48, times=range(60, 421, 30), kee
 
 
 def samples(start: int = 0, n: int | None = None):
-    """(features (n, 40), targets (n, 2), cells (n, 4): x y z d) from the device set."""
+    """(features (n, 40), targets (n, 4): a_p a_q b_p b_q, cells (n, 4): x y z
+    face+8d) from the device set."""
     lib = _lib.load()
     have = int(lib.FLETCHER_AbcSamples())
     n = have - start if n is None else n
     f = np.empty((n, 40), np.float32)
-    t = np.empty((n, 2), np.float32)
+    t = np.empty((n, 4), np.float32)
     c = np.empty((n, 4), np.int32)
     _ok(lib, lib.FLETCHER_AbcGetSamples(start, n, fptr(f), fptr(t), iptr(c)), "AbcGetSamples")
     return f, t, c
@@ -115,18 +119,17 @@ def train(iters: int = 3000, batch: int = 8192, lr: float = 3e-3, seed: int = 1,
     return loss
 
 
-def get_weights():
+def get_weights() -> np.ndarray:
     lib = _lib.load()
     p = np.empty(N_PARAMS, np.float32)
-    s = C.c_float(0)
-    _ok(lib, lib.FLETCHER_AbcGetWeights(fptr(p), C.cast(C.pointer(s), _lib.FP)), "AbcGetWeights")
-    return p, float(s.value)
+    _ok(lib, lib.FLETCHER_AbcGetWeights(fptr(p)), "AbcGetWeights")
+    return p
 
 
-def set_weights(params, out_scale: float) -> None:
+def set_weights(params) -> None:
     lib = _lib.load()
     p = np.ascontiguousarray(params, np.float32)
-    _ok(lib, lib.FLETCHER_AbcSetWeights(fptr(p), float(out_scale)), "AbcSetWeights")
+    _ok(lib, lib.FLETCHER_AbcSetWeights(fptr(p)), "AbcSetWeights")
 
 
 def gradient(features, targets):
@@ -158,28 +161,78 @@ def wide_padding(steps: int, dt: float = 0.0006, dx: float = 12.5) -> int:
 
 
 def boundary_problem(kind: str, n: int, steps: int, seed: int = 1) -> Problem:
-    pad = {"wide": wide_padding(steps), "random": RANDOM_ABSORB, "learned": LAYER, "sponge": LAYER,
-           "plain8": LAYER}[kind]
+    kind, _ = _split_kind(kind)
+    pad = {"wide": wide_padding(steps), "random": RANDOM_ABSORB}.get(kind, LAYER)
     s = n + 2 * (4 + pad)
     return Problem(f"abc-{kind}-{n}", n, n, n, absorb=pad, bord=4, dt=0.0006, steps=steps, fcut=45.0,
                    kind="layered", seed=seed, source=(s // 2, s // 2, 4 + pad + 8))
 
 
-def run_boundary(kind: str, n: int, steps: int, snaps, seed: int = 1, stream=None, damping: float = DAMPING):
-    """Runs one boundary form; returns (interior p at each snapshot step,
-    device ms per step (CUDA events), kernel launches per step)."""
-    import torch
+def _split_kind(kind: str):
+    """'learned@N' -> ('learned', N): the network every N steps."""
+    base, _, n = kind.partition("@")
+    return base, int(n) if n else 1
 
-    prob = boundary_problem(kind, n, steps, seed)
-    model = prob.model() if kind == "random" else prob.raw_model()
-    st = torch.cuda.Stream() if stream is None else stream
-    prop = Propagator(stream=st.cuda_stream)
-    prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model)
-    lib = prop.lib
+
+def _set_boundary(lib, kind: str, damping: float) -> None:
+    kind, interval = _split_kind(kind)
+    _ok(lib, lib.FLETCHER_AbcSetInterval(interval), "AbcSetInterval")
     if kind == "learned":
         _ok(lib, lib.FLETCHER_SetBoundary(BOUNDARY_LEARNED, LAYER, damping), "SetBoundary")
+    elif kind == "oneway":
+        _ok(lib, lib.FLETCHER_SetBoundary(BOUNDARY_ONEWAY, LAYER, damping), "SetBoundary")
     elif kind == "sponge":
         _ok(lib, lib.FLETCHER_SetBoundary(BOUNDARY_SPONGE, LAYER, damping if damping > 0 else 0.03), "SetBoundary")
+
+
+def tuned_shape(kind: str, prob, model, damping: float = DAMPING, steps_per_shape: int = 4, stream=None):
+    """(tile rows, stages) that the library's tuner (FLETCHER_Autotune) picks
+    for this form's grid, boundary launches included, from a short untimed
+    run."""
+    import os
+    import shutil
+    import tempfile
+
+    lib = _lib.load()
+    prop = Propagator(stream=stream)
+    prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model)
+    _set_boundary(lib, kind, damping)
+    tmp = tempfile.mkdtemp(prefix="flt-tune-")
+    rows, stages = C.c_int(0), C.c_int(0)
+    try:
+        rc = lib.FLETCHER_Autotune(os.path.join(tmp, "configurations.txt").encode(), steps_per_shape)
+        _ok(lib, rc not in (0, 1), "Autotune")
+        src = prob.sources(200)
+        t = 0
+        while lib.FLETCHER_GetTileConfig(C.byref(rows), C.byref(stages)) == 1 and t < 200:
+            prop.run(5, prob.i_source, src[t:t + 5])
+            t += 5
+        prop.synchronize()
+        lib.FLETCHER_GetTileConfig(C.byref(rows), C.byref(stages))
+    finally:
+        lib.FLETCHER_SetBoundary(BOUNDARY_PLAIN, 0, 0.0)
+        lib.FLETCHER_AbcSetInterval(1)
+        prop.finalize()
+        shutil.rmtree(tmp, ignore_errors=True)
+    return int(rows.value), int(stages.value)
+
+
+def run_boundary(kind: str, n: int, steps: int, snaps, seed: int = 1, stream=None, damping: float = DAMPING,
+                 tune: bool = True):
+    """Runs one boundary form (with its tuned tile shape when `tune`);
+    returns (interior p at each snapshot step, device ms per step (CUDA
+    events), kernel launches per step, tile shape)."""
+    import torch
+
+    base, _ = _split_kind(kind)
+    prob = boundary_problem(base, n, steps, seed)
+    model = prob.model() if base == "random" else prob.raw_model()
+    st = torch.cuda.Stream() if stream is None else stream
+    shape = tuned_shape(kind, prob, model, damping, stream=st.cuda_stream) if tune else (0, 0)
+    prop = Propagator(*shape, stream=st.cuda_stream)
+    prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model)
+    lib = prop.lib
+    _set_boundary(lib, kind, damping)
     src = prob.sources(steps)
     o = prob.bord + prob.absorb
     out = []
@@ -195,10 +248,16 @@ def run_boundary(kind: str, n: int, steps: int, snaps, seed: int = 1, stream=Non
         t0 = t
         p = prop.field(0).reshape(prob.sz, prob.sy, prob.sx)
         out.append(np.ascontiguousarray(p[o:o + n, o:o + n, o:o + n]))
-    if kind in ("learned", "sponge"):
-        lib.FLETCHER_SetBoundary(BOUNDARY_PLAIN, 0, 0.0)
+    rows, stages = C.c_int(0), C.c_int(0)
+    lib.FLETCHER_GetTileConfig(C.byref(rows), C.byref(stages))
+    lib.FLETCHER_SetBoundary(BOUNDARY_PLAIN, 0, 0.0)
+    lib.FLETCHER_AbcSetInterval(1)
     prop.finalize()
-    return out, ms / max(snaps), {"learned": 3, "sponge": 2}.get(kind, 1)
+    Propagator()  # back to the default tile shape
+    _, interval = _split_kind(kind)
+    extra = {"learned": 3 + 1.0 / interval, "oneway": 3, "sponge": 1}.get(base, 0)
+    extra += 1 if damping > 0 and base in ("learned", "oneway") else 0
+    return out, ms / max(snaps), 1 + extra, (rows.value, stages.value)
 
 
 def reflected_energy(fields, reference) -> float:
@@ -207,19 +266,20 @@ def reflected_energy(fields, reference) -> float:
     return num / den
 
 
-def compare(n: int = 256, steps: int = 1500, nsnap: int = 5, kinds=("random", "learned", "sponge", "plain8"),
-            seed: int = 1, damping: float = DAMPING):
+def compare(n: int = 256, steps: int = 1500, nsnap: int = 5, kinds=("random", "learned", "oneway", "plain8"),
+            seed: int = 1, damping: float = DAMPING, tune: bool = True):
     """Reflected energy (total and per snapshot) and interior MSamples/s of
-    each boundary form."""
+    each boundary form, each run with the tile shape the tuner picks for it
+    (`tune`)."""
     snaps = [int(round(steps * (k + 1) / nsnap)) for k in range(nsnap)]
-    ref, ref_ms, _ = run_boundary("wide", n, steps, snaps, seed)
+    ref, ref_ms, _, ref_shape = run_boundary("wide", n, steps, snaps, seed, tune=tune)
     res = {"wide": {"ms_per_step": ref_ms, "interior_msamples": n ** 3 / ref_ms / 1e3, "reflected_energy": 0.0,
-                    "padding": wide_padding(steps)}}
+                    "padding": wide_padding(steps), "tile": list(ref_shape)}}
     for k in kinds:
-        f, ms, launches = run_boundary(k, n, steps, snaps, seed, damping=damping)
+        f, ms, launches, shape = run_boundary(k, n, steps, snaps, seed, damping=damping, tune=tune)
         res[k] = {"ms_per_step": ms, "interior_msamples": n ** 3 / ms / 1e3,
                   "reflected_energy": reflected_energy(f, ref),
                   "reflected_energy_by_snapshot": [reflected_energy([a], [b]) for a, b in zip(f, ref)],
-                  "launches_per_step": launches}
+                  "launches_per_step": launches, "tile": list(shape)}
     res["snapshots"] = snaps
     return res

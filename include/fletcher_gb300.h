@@ -106,8 +106,23 @@ int FLETCHER_HostAccess(void);
 int FLETCHER_SetForm(int form);
 
 /* Kernel shape override for tuning (0 keeps the default): rows per tile,
- * pipeline stages, z-chunks per column. */
+ * pipeline stages, z-chunks per column (> 0: that many, the last partial
+ * round of items shared out over the CTAs; < 0: -zchunks, all items
+ * round-robin). */
 int FLETCHER_SetTileConfig(int tile_rows, int stages, int zchunks);
+
+/* The work split of a single-shot launch (host only): ntx x nty tiles of
+ * 32 x tile_rows cells, planes [zlo, zlo + depth), over `ctas` persistent
+ * CTAs.  Whole rounds of z-chunks go round-robin (CTAs side by side on
+ * neighbouring tiles); the last partial round is shared out in equal
+ * pieces of at least 8 planes.  Writes the segments {x0, y0, z0, z1} CTA by
+ * CTA into seg_out (when they fit in `cap`), each CTA's first segment into
+ * first_out [ctas + 1], and the busiest CTA's cost (its planes plus 4 a
+ * segment for the halo, shared-out pieces counting 3/2) into max_cost;
+ * returns the segment count (negative on error).  zchunks as in
+ * FLETCHER_SetTileConfig (0: the cheapest plan). */
+int FLETCHER_PlanSegments(int ctas, int ntx, int nty, int tile_rows, int zlo, int depth, int zchunks, int *seg_out,
+                          int cap, int *first_out, long *max_cost);
 
 /* Tile-shape tuning with a configuration file in the format of the
  * reference's block-size tuner (original_singleGPU_PDP/model.c:51-113,
@@ -307,66 +322,75 @@ int FLETCHER_Model(int st, long iSource, double fcut, float dt_output, int sx, i
  *
  * The grid is interior + a layer of L cells + bord on every side, the medium
  * extended into the layer.  The plain update covers interior and layer; the
- * layer's face cells more than L - 4 cells outside the interior (whose
- * stencils reach the zero border) get a correction from a per-cell MLP
- * (40 -> 32 -> 32 -> 2, tanh, FP16 weights, FP32 accumulation) that predicts
- * the update's contribution of an unbounded medium beyond the layer.
- * Inputs: the 9-point outward-normal stencils of p and q at t and t-1
- * (scaled by their largest magnitude s), vpz / 4000, epsilon, delta, d / L;
- * the correction is s * out_scale * output.  FLETCHER_ABC_PARAMS master
- * weights (FP32): W1 [32][40], b1 [32], W2 [32][32], b2 [32], W3 [2][32],
- * b3 [2]. */
+ * layer's outer 4 cells (the ghost zone: d = L-3 .. L cells outside the
+ * interior, whose stencils reach the zero border) are then overwritten with
+ * the box-scheme update of the one-way wave equation along the outward
+ * normal, u_g(t+1) = u_i(t) + k (u_g(t) - u_i(t+1)) (g the cell, i its
+ * inward neighbour), outward from d = L-3, z faces, then y, then x.
+ * FLETCHER_BOUNDARY_ONEWAY takes k = (1 - r) / (1 + r), r = c dt / h, from
+ * the medium (c = vpz along z, vpz sqrt(1 + 2 eps) along x and y);
+ * FLETCHER_BOUNDARY_LEARNED takes (k_p, k_q) = sigmoid(y) of a per-cell MLP
+ * (40 -> 32 -> 32 -> 2, tanh, FP16 weights, FP32 accumulation) evaluated
+ * every step.  Inputs: the 9-point outward-normal stencils of p and q at t
+ * and t-1 (points beyond the layer read as zero, all divided by their
+ * largest magnitude s), vpz / 4000, epsilon, delta, d / L.
+ * FLETCHER_ABC_PARAMS master weights (FP32): W1 [32][40], b1 [32],
+ * W2 [32][32], b2 [32], W3 [2][32], b3 [2]. */
 #define FLETCHER_ABC_PARAMS 2434
 #define FLETCHER_BOUNDARY_PLAIN 0
 #define FLETCHER_BOUNDARY_LEARNED 1
 #define FLETCHER_BOUNDARY_SPONGE 2
+#define FLETCHER_BOUNDARY_ONEWAY 3
 
-/* Network weights: random initialisation (Xavier, seeded), set, get. */
+/* Network weights: random initialisation (Xavier, seeded; output biases
+ * start at k ~ 0.7), set, get. */
 int FLETCHER_AbcInit(unsigned seed);
-int FLETCHER_AbcSetWeights(const float *params, float out_scale);
-int FLETCHER_AbcGetWeights(float *params, float *out_scale);
+int FLETCHER_AbcSetWeights(const float *params);
+int FLETCHER_AbcGetWeights(float *params);
 
 /* Training set on the device: AbcReserve(capacity) (re)allocates and
  * empties it; AbcCollect appends samples from the resident FP32 state (its
  * current and previous fields): around the interior box [lo, hi) with a
- * layer of `layer` cells, a random fraction keep_frac of the network's layer
- * cells whose stencil magnitude exceeds min_scale, each with its 40 inputs
- * and target (the contribution of the cells beyond the layer to the cell's
- * next p and q, over s).  The box, its layer and 4 more cells must lie in
- * the updated region. */
+ * layer of `layer` cells, a random fraction keep_frac of the ghost cells
+ * whose stencil magnitude s exceeds min_scale, each with its 40 inputs and
+ * targets a = (u_g(t) - u_i(t+1)) / s, b = (u_g(t+1) - u_i(t)) / s for p
+ * and q, u(t+1) being the plain update on the resident field.  The box, its
+ * layer and 4 more cells must lie in the updated region. */
 int FLETCHER_AbcReserve(long capacity);
 int FLETCHER_AbcCollect(const int *interior_lo, const int *interior_hi, int layer, float keep_frac, unsigned seed,
                         float min_scale);
 long FLETCHER_AbcSamples(void);
-/* Samples [start, start + n): features [n][40], targets [n][2], and the
- * cell of each (x, y, z, d: [n][4] ints); any pointer may be NULL. */
+/* Samples [start, start + n): features [n][40], targets [n][4] (a_p, a_q,
+ * b_p, b_q), and the cell of each ([n][4] ints: x, y, z, face + 8 d; faces
+ * 0..5 are z-, z+, y-, y+, x-, x+); any pointer may be NULL. */
 int FLETCHER_AbcGetSamples(long start, long n, float *features, float *targets, int *cells);
 
 /* iters Adam steps (cosine-decayed learning rate from lr) on random batches
  * of `batch` samples, the stencil inputs perturbed by noise of standard
- * deviation `noise` (0: none); the first training of a set of weights fixes
- * out_scale to the targets' root mean square.  loss_out: iters losses. */
+ * deviation `noise` (0: none).  loss_out: iters losses. */
 int FLETCHER_AbcTrain(int iters, int batch, float lr, unsigned seed, float noise, float *loss_out);
 
 /* One forward and backward pass on n given samples (features [n][40],
- * targets [n][2], compared with the raw outputs): loss = sum (y - t)^2 /
- * (2 n) and its gradient with respect to the master weights. */
+ * targets [n][4]): loss = sum_c (sigmoid(y_c) a_c - b_c)^2 / (2 n) and its
+ * gradient with respect to the master weights. */
 int FLETCHER_AbcGradient(const float *features, const float *targets, int n, float *grad, float *loss);
 
 /* The inference path (tensor cores) on n given feature rows: raw outputs
- * [n][2]. */
+ * y [n][2] (k = sigmoid(y)). */
 int FLETCHER_AbcForward(const float *features, int n, float *out);
 
-/* Boundary of the resident FP32 state.  FLETCHER_BOUNDARY_PLAIN: none.
- * FLETCHER_BOUNDARY_LEARNED: a layer of `layer` cells (>= 5) inside the
- * updated region (interior = updated region shrunk by `layer`) whose outer
- * face cells get the network's correction; each step then also launches the
- * layer's inference kernel (before the propagate kernel) and an add kernel
- * (after it).  damping > 0 also scales every layer cell by exp(-(damping *
- * d)^2) after the step.  FLETCHER_BOUNDARY_SPONGE: the same layer with that
- * scaling only (damping > 0), no network.  FLETCHER_AbcLayerCells: cells
- * the network evaluates per step. */
+/* Boundary of the resident FP32 state, a layer of `layer` cells (>= 5)
+ * inside the updated region (interior = updated region shrunk by `layer`).
+ * FLETCHER_BOUNDARY_PLAIN: none.  FLETCHER_BOUNDARY_ONEWAY and
+ * FLETCHER_BOUNDARY_LEARNED: the ghost-zone update after every step (three
+ * launches; the learned form adds one inference launch before the step).
+ * damping > 0 also scales every layer cell by exp(-(damping d)^2) after the
+ * step; FLETCHER_BOUNDARY_SPONGE is that scaling alone (damping > 0).
+ * FLETCHER_AbcLayerCells: ghost cells updated per step (one-way forms). */
 int FLETCHER_SetBoundary(int mode, int layer, float damping);
+/* The learned form evaluates the network every `steps` steps (default 1)
+ * and keeps the last coefficients in between (counted from SetBoundary). */
+int FLETCHER_AbcSetInterval(int steps);
 long FLETCHER_AbcLayerCells(void);
 void FLETCHER_AbcRelease(void);
 

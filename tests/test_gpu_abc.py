@@ -6,13 +6,14 @@ the CPU oracle (oracle/abc_mlp.py).
   accumulation);
 * the tensor-core inference path vs the oracle's forward: within 3e-2 of
   the outputs' RMS (tanh.approx and FP16 rounding of the activations);
-* collected training samples (features and targets of layer cells) vs the
-  oracle's restatement at the same cells: 1e-5;
-* one step of the resident learned layer (fused gather + network + add):
-  its change at every network cell equals the oracle's network on the
-  oracle's inputs for that cell (3e-2 of the RMS), nothing else changes;
-* end to end on a small case: training lowers the loss, and the
-  reflected-energy harness measures every boundary form.
+* collected training samples (features and targets of ghost cells) vs the
+  oracle's restatement at the same cells;
+* one step of the resident one-way layer: the fixed-coefficient form equals
+  the oracle's box-scheme update of the plain step (1e-6), the learned form
+  equals it with the oracle network's coefficients (1e-2 of the update's
+  size), and nothing outside the ghost zone changes;
+* end to end on a small case: training lowers the loss, the one-way forms
+  stay stable, and the reflected-energy harness measures every form.
 """
 import numpy as np
 import pytest
@@ -52,9 +53,9 @@ def test_gradient_vs_cpu_oracle():
     from oracle import abc_mlp
 
     learned.init(3)
-    P, _ = learned.get_weights()
+    P = learned.get_weights()
     X = random_features(300, 1)
-    T = np.random.default_rng(2).normal(0, 1, (300, 2)).astype(np.float32)
+    T = np.random.default_rng(2).normal(0, 1, (300, 4)).astype(np.float32)
     loss, g = learned.gradient(X, T)
     oloss, og = abc_mlp.loss_and_grad(P, X, T)
     assert abs(loss - oloss) <= 1e-4 * oloss
@@ -67,7 +68,7 @@ def test_inference_path_vs_cpu_oracle():
     from oracle import abc_mlp
 
     learned.init(4)
-    P, _ = learned.get_weights()
+    P = learned.get_weights()
     X = random_features(1000, 5)  # not a multiple of 16: the last tile is partial
     y = learned.forward(X)
     oy, _ = abc_mlp.forward(P, X)
@@ -94,93 +95,140 @@ def test_collected_samples_vs_cpu_restatement():
     prev = np.stack([prop.field(2).reshape(shape), prop.field(3).reshape(shape)])
     coef = prop.coefficients().reshape((10,) + shape)
     prop.finalize()
-    # every outer face cell with a wave on it, once
-    assert len(f) > 1000 and len({tuple(c[:3]) for c in cells}) == len(f)
+    # every ghost cell with a wave on it, once
+    ghost = {c[:3] + (c[3] + 8 * c[4],) for c in abc_mlp.ghost_cells(lo, hi, learned.LAYER)}
+    got = {tuple(int(v) for v in c) for c in cells}
+    assert len(f) > 1000 and len(got) == len(f) and got <= ghost
     pick = np.random.default_rng(0).choice(len(f), 200, replace=False)
-    of, ot = abc_mlp.features_targets(cur, prev, coef, lo, hi, learned.LAYER, [tuple(c[:3]) for c in cells[pick]],
-                                      (prob.dx, prob.dy, prob.dz), prob.dt)
+    sel = [(int(c[0]), int(c[1]), int(c[2]), int(c[3]) % 8, int(c[3]) // 8) for c in cells[pick]]
+    of, ot = abc_mlp.features_targets(cur, prev, coef, lo, hi, learned.LAYER, sel, (prob.dx, prob.dy, prob.dz),
+                                      prob.dt)
     assert np.max(np.abs(f[pick] - of)) < 1e-5
-    assert np.max(np.abs(t[pick] - ot)) < 1e-5 * np.max(np.abs(ot)) + 1e-12
-    assert np.all(cells[pick, 3] > learned.LAYER - 4)
+    # a and b are differences of O(1) values (over s): FP32 rounding of the update
+    assert np.max(np.abs(t[pick] - ot)) < 1e-5 * np.max(np.abs(ot)) + 1e-5
 
 
-def test_fused_layer_step_vs_cpu_oracle():
-    """One step of the resident learned layer: the change it makes at each
-    network cell (vs the same step without the layer) equals the oracle's
-    network on the oracle's inputs for that cell, times s * out_scale."""
+def _one_step(prob, model, fields, mode):
+    prop = Propagator()
+    prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model, *fields)
+    assert prop.lib.FLETCHER_SetBoundary(mode, learned.LAYER, 0.0) == 0
+    ncells = prop.lib.FLETCHER_AbcLayerCells()
+    prop.run(1)
+    prop.synchronize()
+    out = np.stack([prop.field(0), prop.field(1)])
+    prop.lib.FLETCHER_SetBoundary(learned.BOUNDARY_PLAIN, 0, 0.0)
+    prop.finalize()
+    return out, ncells
+
+
+def test_resident_oneway_steps_vs_cpu_oracle():
+    """One step with the fixed-coefficient and the learned ghost zone: the
+    plain step followed by the oracle's box-scheme update (with the
+    medium's coefficients, and with sigmoid of the oracle network on the
+    oracle's inputs), and no change outside the ghost zone."""
     from oracle import abc_mlp
 
     learned.init(6)
-    P, scale = learned.get_weights()
-    prob = learned.boundary_problem("learned", 24, 120)
+    P = learned.get_weights()
+    prob = learned.boundary_problem("learned", 16, 150)
     model = prob.raw_model()
     prop = Propagator()
     prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model)
-    prop.run(120, prob.i_source, prob.sources(120))
+    prop.run(150, prob.i_source, prob.sources(150))
     prop.synchronize()
     f = [prop.field(k) for k in (2, 0, 3, 1)]  # pp pc qp qc
     coef = prop.coefficients()
     prop.finalize()
-    out = []
-    for mode in (learned.BOUNDARY_PLAIN, learned.BOUNDARY_LEARNED):
-        prop = Propagator()
-        prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model, *f)
-        assert prop.lib.FLETCHER_SetBoundary(mode, learned.LAYER, 0.0) == 0
-        ncells = prop.lib.FLETCHER_AbcLayerCells()
-        prop.run(1)
-        prop.synchronize()
-        out.append((prop.field(0), prop.field(1)))
-        prop.lib.FLETCHER_SetBoundary(learned.BOUNDARY_PLAIN, 0, 0.0)
-        prop.finalize()
     shape = (prob.sz, prob.sy, prob.sx)
-    dp = (out[1][0] - out[0][0]).reshape(shape)
-    dq = (out[1][1] - out[0][1]).reshape(shape)
+    plain, _ = _one_step(prob, model, f, learned.BOUNDARY_PLAIN)
+    fixed, n_fixed = _one_step(prob, model, f, learned.BOUNDARY_ONEWAY)
+    lrn, n_lrn = _one_step(prob, model, f, learned.BOUNDARY_LEARNED)
     b, L = prob.bord, learned.LAYER
     lo, hi = (b + L,) * 3, (prob.sx - b - L, prob.sy - b - L, prob.sz - b - L)
-    # the network's cells: more than L - 4 outside the interior along exactly one axis
-    cells = []
-    for z in range(b, prob.sz - b):
-        for y in range(b, prob.sy - b):
-            for x in range(b, prob.sx - b):
-                far = sum(1 for c, l, h in zip((x, y, z), lo, hi) if c < l - (L - 4) or c >= h + (L - 4))
-                if far == 1:
-                    cells.append((x, y, z))
-    assert ncells == len(cells)
-    cur = np.stack([f[1].reshape(shape), f[3].reshape(shape)])
-    prev = np.stack([f[0].reshape(shape), f[2].reshape(shape)])
-    pick = [cells[i] for i in np.random.default_rng(1).choice(len(cells), 300, replace=False)]
-    X, _, sc = abc_mlp.features_targets(cur, prev, coef.reshape((10,) + shape), lo, hi, L, pick,
-                                        (prob.dx, prob.dy, prob.dz), prob.dt, return_scale=True)
-    y, _ = abc_mlp.forward(P, X)
-    want = y * (sc * scale)[:, None]
-    got = np.array([[dp[z, y_, x], dq[z, y_, x]] for (x, y_, z) in pick])
-    rms = np.sqrt(np.mean(want ** 2))
-    assert rms > 0
-    assert np.max(np.abs(got - want)) < 3e-2 * rms + 1e-6 * np.abs(cur).max()
-    # nothing else changes
+    cells = abc_mlp.ghost_cells(lo, hi, L)
+    assert n_fixed == n_lrn == len(cells)
+    cur = np.stack([f[1].reshape(shape), f[3].reshape(shape)]).astype(np.float64)
+    prev = np.stack([f[0].reshape(shape), f[2].reshape(shape)]).astype(np.float64)
+    base = plain.reshape((2,) + shape).astype(np.float64)
     mask = np.zeros(shape, bool)
-    for (x, y_, z) in cells:
-        mask[z, y_, x] = True
-    assert not np.any(dp[~mask]) and not np.any(dq[~mask])
+    for (x, y, z, _, _) in cells:
+        mask[z, y, x] = True
+    scale = np.abs(cur).max()
+    assert scale > 0
+    # fixed coefficients, from the medium in FP32 as the library computes them
+    c4 = coef.reshape((10,) + shape)
+    k = np.empty((len(cells), 2))
+    dt, h = np.float32(prob.dt), (prob.dx, prob.dy, prob.dz)
+    for i, (x, y, z, fc, d) in enumerate(cells):
+        v2pz, v2px = np.float32(c4[7, z, y, x]), np.float32(c4[6, z, y, x])
+        vpz = np.sqrt(v2pz)
+        eps = np.float32(0.5) * (v2px / v2pz - np.float32(1))
+        a = abc_mlp.face_axis(fc)
+        c = vpz if a == 2 else vpz * np.sqrt(np.float32(1) + np.float32(2) * eps)
+        r = c * dt / np.float32(h[a])
+        k[i] = (1 - r) / (1 + r)
+    want = abc_mlp.oneway_update(cur, base.copy(), lo, hi, L, k)
+    got = fixed.reshape((2,) + shape)
+    assert np.max(np.abs(got - want)) < 1e-6 * scale
+    assert np.array_equal(got[:, ~mask], plain.reshape((2,) + shape)[:, ~mask])
+    # learned coefficients
+    X, _ = abc_mlp.features_targets(cur, prev, c4, lo, hi, L, cells, h, prob.dt, targets=False)
+    y, _ = abc_mlp.forward(P, X)
+    want = abc_mlp.oneway_update(cur, base.copy(), lo, hi, L, abc_mlp.sigmoid(y))
+    got = lrn.reshape((2,) + shape)
+    size = np.max(np.abs(want - base)[:, mask])
+    assert size > 0
+    assert np.max(np.abs(got - want)) < 1e-2 * size + 1e-6 * scale
+    assert np.array_equal(got[:, ~mask], plain.reshape((2,) + shape)[:, ~mask])
 
 
 def test_training_and_reflected_energy_small():
-    """Training on small padded models lowers the loss; the reflected-energy
-    harness measures every boundary form against the wide-domain run.  The
-    32-cell random shell reflects less than the bare 8-cell layer; the
-    learned layer's numbers are reported, not bounded (the network, fed the
-    fields at t and t-1 only, has to extrapolate the wave up to 4 cells past
-    the layer, and its error grows through the feedback of the layer's own
-    values)."""
+    """Training on small padded models lowers the loss; the one-way forms
+    stay bounded and reflect less than the bare 8-cell layer; the harness
+    measures every form against the wide-domain run."""
     n_s = learned.collect(models=12, n_virtual=32, times=range(40, 281, 20), keep=0.3, capacity=2_000_000)
     assert n_s > 30000
     learned.init(0)
     loss = learned.train(iters=800, batch=4096, lr=3e-3)
     print(f"samples {n_s}, loss {loss[:20].mean():.4g} -> {loss[-50:].mean():.4g}")
-    assert loss[-50:].mean() < 0.3 * loss[:20].mean()
+    assert loss[-50:].mean() < 0.7 * loss[:20].mean()
     res = learned.compare(n=48, steps=600, nsnap=3)
     for k, v in res.items():
         print(k, v)
     assert res["wide"]["reflected_energy"] == 0.0
-    assert 0.0 < res["random"]["reflected_energy"] < res["plain8"]["reflected_energy"]
-    assert res["learned"]["launches_per_step"] == 3
+    plain = res["plain8"]["reflected_energy"]
+    assert 0.0 < res["random"]["reflected_energy"] < plain
+    assert 0.0 < res["oneway"]["reflected_energy"] < plain
+    assert 0.0 < res["learned"]["reflected_energy"] < plain
+    assert res["learned"]["launches_per_step"] == 5 and res["oneway"]["launches_per_step"] == 4
+
+
+def test_interval_reuses_the_coefficients():
+    """With the network every 2 steps the first step equals the every-step
+    run bit for bit (both evaluate it), the second differs (it reuses the
+    first step's coefficients)."""
+    learned.init(7)
+    prob = learned.boundary_problem("learned", 16, 150)
+    model = prob.raw_model()
+    prop = Propagator()
+    prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model)
+    prop.run(150, prob.i_source, prob.sources(150))
+    prop.synchronize()
+    f = [prop.field(k) for k in (2, 0, 3, 1)]
+    prop.finalize()
+    out = {}
+    for interval in (1, 2):
+        prop = Propagator()
+        prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model, *f)
+        assert prop.lib.FLETCHER_AbcSetInterval(interval) == 0
+        assert prop.lib.FLETCHER_SetBoundary(learned.BOUNDARY_LEARNED, learned.LAYER, 0.0) == 0
+        prop.run(1)
+        a = prop.field(0)
+        prop.run(1)
+        out[interval] = (a, prop.field(0))
+        prop.lib.FLETCHER_SetBoundary(learned.BOUNDARY_PLAIN, 0, 0.0)
+        prop.lib.FLETCHER_AbcSetInterval(1)
+        prop.finalize()
+    assert np.array_equal(out[1][0], out[2][0])
+    assert not np.array_equal(out[1][1], out[2][1])
+    assert np.max(np.abs(out[1][1] - out[2][1])) < 0.1 * np.max(np.abs(out[1][1]))
