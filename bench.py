@@ -395,7 +395,7 @@ def run_learned_form(args, ws, rank, local, group):
     t2 = time.time()
     n, steps = args.abc_interior, args.abc_steps
     res = learned.compare(n=n, steps=steps, nsnap=5,
-                          kinds=("random", "learned", "learned@2", "learned@4", "oneway", "plain8"))
+                          kinds=("random", "learned", "learned@2", "learned@4", "learned@8", "oneway", "plain8"))
     group.barrier()
     if rank != 0:
         return

@@ -168,6 +168,24 @@ __host__ __device__ __forceinline__ long cell_index(int x, int y, int z, int sy,
   return ((long)z * sy + y) * pitch + x;
 }
 
+// Index in the field of ghost cell i and its face (ghost_cell without an
+// indexed coordinate array, for the hot kernels).
+__device__ __forceinline__ long ghost_index(const Ghost &G, long i, int sy, int pitch, int &f) {
+  f = face_of(G, i);
+  const long j = i - G.off[f];
+  const int a = face_axis(f);
+  const int t0 = a == 0 ? 1 : 0, t1 = a == 2 ? 1 : 2;
+  const int e0 = G.keep.hi[t0] - G.keep.lo[t0];
+  const int ray = (int)(j / kGhostD);
+  const int d = G.L - kGhostD + 1 + (int)(j % kGhostD);
+  const int u = G.keep.lo[t0] + ray % e0, v = G.keep.lo[t1] + ray / e0;
+  const int n = face_sign(f) < 0 ? G.in.lo[a] - d : G.in.hi[a] - 1 + d;
+  const int x = a == 0 ? n : u;
+  const int y = a == 1 ? n : (a == 0 ? u : v);
+  const int z = a == 2 ? n : v;
+  return cell_index(x, y, z, sy, pitch);
+}
+
 // ---- features -------------------------------------------------------------------
 
 // vpz, epsilon, delta of a cell from its coefficients (v2pz = vpz^2,
@@ -360,9 +378,54 @@ __device__ __forceinline__ uint32_t tanh_h2(float lo_v, float hi_v) {
   return y;
 }
 
+// A lane's share of the network for mma.sync m16n8k16: the B fragments of
+// the three layers and the biases of the output columns it holds (g = lane
+// / 4 selects the row of B, t = lane % 4 the column pair).  Loaded once per
+// warp, kept in registers.
+struct Frags {
+  uint32_t w1[4][3][2];  // layer 1: n-tile, k-step, (k 2t, k 2t+8)
+  uint32_t w2[4][2][2];  // layer 2
+  uint32_t w3[2][2];     // layer 3 (n-tile 0)
+  float b1[4][2], b2[4][2], b3[2];
+};
+
+__device__ __forceinline__ void load_frags(const NetHalf *__restrict__ N, Frags &F) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const uint32_t *w1 = reinterpret_cast<const uint32_t *>(N->w1);
+  const uint32_t *w2 = reinterpret_cast<const uint32_t *>(N->w2);
+  const uint32_t *w3 = reinterpret_cast<const uint32_t *>(N->w3);
+#pragma unroll
+  for (int nt = 0; nt < 4; ++nt) {
+#pragma unroll
+    for (int ks = 0; ks < 3; ++ks) {
+      const int o = ((8 * nt + g) * kK1 + 16 * ks + 2 * t) / 2;
+      F.w1[nt][ks][0] = w1[o];
+      F.w1[nt][ks][1] = w1[o + 4];
+    }
+#pragma unroll
+    for (int kt = 0; kt < 2; ++kt) {
+      const int o = ((8 * nt + g) * kHid + 16 * kt + 2 * t) / 2;
+      F.w2[nt][kt][0] = w2[o];
+      F.w2[nt][kt][1] = w2[o + 4];
+    }
+    F.b1[nt][0] = N->b1[8 * nt + 2 * t];
+    F.b1[nt][1] = N->b1[8 * nt + 2 * t + 1];
+    F.b2[nt][0] = N->b2[8 * nt + 2 * t];
+    F.b2[nt][1] = N->b2[8 * nt + 2 * t + 1];
+  }
+#pragma unroll
+  for (int kt = 0; kt < 2; ++kt) {
+    const int o = (g * kHid + 16 * kt + 2 * t) / 2;
+    F.w3[kt][0] = w3[o];
+    F.w3[kt][1] = w3[o + 4];
+  }
+  F.b3[0] = N->b3[2 * t];
+  F.b3[1] = N->b3[2 * t + 1];
+}
+
 // The network on the warp's 16-row feature tile Xs (FP16, row stride kXs).
 // Lanes with (lane & 3) == 0 return the outputs of rows lane/4 and lane/4+8.
-__device__ __forceinline__ void mlp16(const __half *Xs, const NetHalf &N, float (&y_lo)[2], float (&y_hi)[2]) {
+__device__ __forceinline__ void mlp16(const __half *Xs, const Frags &F, float (&y_lo)[2], float (&y_hi)[2]) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   uint32_t a[3][4];
 #pragma unroll
@@ -375,13 +438,9 @@ __device__ __forceinline__ void mlp16(const __half *Xs, const NetHalf &N, float 
   float h[4][4];
 #pragma unroll
   for (int nt = 0; nt < 4; ++nt) {
-    const float b0 = N.b1[8 * nt + 2 * t], b1 = N.b1[8 * nt + 2 * t + 1];
-    h[nt][0] = b0; h[nt][1] = b1; h[nt][2] = b0; h[nt][3] = b1;
+    h[nt][0] = F.b1[nt][0]; h[nt][1] = F.b1[nt][1]; h[nt][2] = F.b1[nt][0]; h[nt][3] = F.b1[nt][1];
 #pragma unroll
-    for (int ks = 0; ks < 3; ++ks) {
-      const __half *w = N.w1 + (8 * nt + g) * kK1 + 16 * ks + 2 * t;
-      mma16816(h[nt], a[ks], *reinterpret_cast<const uint32_t *>(w), *reinterpret_cast<const uint32_t *>(w + 8));
-    }
+    for (int ks = 0; ks < 3; ++ks) mma16816(h[nt], a[ks], F.w1[nt][ks][0], F.w1[nt][ks][1]);
   }
   uint32_t a2[2][4];
 #pragma unroll
@@ -393,13 +452,9 @@ __device__ __forceinline__ void mlp16(const __half *Xs, const NetHalf &N, float 
   }
 #pragma unroll
   for (int nt = 0; nt < 4; ++nt) {
-    const float b0 = N.b2[8 * nt + 2 * t], b1 = N.b2[8 * nt + 2 * t + 1];
-    h[nt][0] = b0; h[nt][1] = b1; h[nt][2] = b0; h[nt][3] = b1;
+    h[nt][0] = F.b2[nt][0]; h[nt][1] = F.b2[nt][1]; h[nt][2] = F.b2[nt][0]; h[nt][3] = F.b2[nt][1];
 #pragma unroll
-    for (int kt = 0; kt < 2; ++kt) {
-      const __half *w = N.w2 + (8 * nt + g) * kHid + 16 * kt + 2 * t;
-      mma16816(h[nt], a2[kt], *reinterpret_cast<const uint32_t *>(w), *reinterpret_cast<const uint32_t *>(w + 8));
-    }
+    for (int kt = 0; kt < 2; ++kt) mma16816(h[nt], a2[kt], F.w2[nt][kt][0], F.w2[nt][kt][1]);
   }
 #pragma unroll
   for (int kt = 0; kt < 2; ++kt) {
@@ -408,12 +463,9 @@ __device__ __forceinline__ void mlp16(const __half *Xs, const NetHalf &N, float 
     a2[kt][2] = tanh_h2(h[2 * kt + 1][0], h[2 * kt + 1][1]);
     a2[kt][3] = tanh_h2(h[2 * kt + 1][2], h[2 * kt + 1][3]);
   }
-  float o[4] = {N.b3[2 * t], N.b3[2 * t + 1], N.b3[2 * t], N.b3[2 * t + 1]};
+  float o[4] = {F.b3[0], F.b3[1], F.b3[0], F.b3[1]};
 #pragma unroll
-  for (int kt = 0; kt < 2; ++kt) {
-    const __half *w = N.w3 + g * kHid + 16 * kt + 2 * t;
-    mma16816(o, a2[kt], *reinterpret_cast<const uint32_t *>(w), *reinterpret_cast<const uint32_t *>(w + 8));
-  }
+  for (int kt = 0; kt < 2; ++kt) mma16816(o, a2[kt], F.w3[kt][0], F.w3[kt][1]);
   y_lo[0] = o[0];
   y_lo[1] = o[1];
   y_hi[0] = o[2];
@@ -429,60 +481,65 @@ __device__ __forceinline__ float sigmoid(float y) { return 1.0f / (1.0f + __expf
 // takes 16 consecutive cells, 4 rays (rays start at multiples of 4 cells).
 // The 4 ghost cells of a ray (d = L-3 .. L) read the 8 points d = L-7 .. L
 // of its normal line (points past the layer read as zero): lane 8r + q
-// loads point q of ray r at t and t-1 once into shared memory; then two
-// lanes per cell, one for each time, build the cell's stencils from it.
+// loads point q of ray r at t and t-1 once into shared memory (the next
+// tile's loads are issued before this tile's network runs); then two lanes
+// per cell, one for each time, build the cell's stencils from it.
 // k[i] = (k_p, k_q).
-__global__ void __launch_bounds__(32 * kInferWarps) k_abc_infer(const __grid_constant__ Ghost G, const float2 *cur, const float2 *prev, int sy,
-                                                                 int pitch, const float4 *med, const NetHalf *net,
-                                                                 float2 *kout) {
+constexpr int kInferBlocksPerSm = 2;  // 128 registers a thread (the network stays in registers)
+
+__global__ void __launch_bounds__(32 * kInferWarps, kInferBlocksPerSm) k_abc_infer(
+    const __grid_constant__ Ghost G, const float2 *__restrict__ cur, const float2 *__restrict__ prev, int sy,
+    int pitch, const float4 *__restrict__ med, const NetHalf *__restrict__ net, float2 *__restrict__ kout) {
   __shared__ __align__(16) __half Xs[kInferWarps][16 * kXs];
-  __shared__ float4 Ln[kInferWarps][4][8];  // (p, q at t, p, q at t-1) of each ray's line points
-  __shared__ NetHalf N;
-  for (int i = threadIdx.x; i < (int)(sizeof(NetHalf) / 4); i += blockDim.x)
-    reinterpret_cast<uint32_t *>(&N)[i] = reinterpret_cast<const uint32_t *>(net)[i];
-  __syncthreads();
+  __shared__ float2 Ln[kInferWarps][2][4][8];  // [time: t, t-1][ray][point] (p, q)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = lane >> 1, half_t = lane & 1;
+  Frags F;
+  load_frags(net, F);
   __half *X = Xs[warp];
   const long ncells = G.off[6];
   const long ntiles = (ncells + 15) / 16;
-  for (long tile = blockIdx.x * (long)kInferWarps + warp; tile < ntiles; tile += (long)gridDim.x * kInferWarps) {
-    {
-      const int ray = lane >> 3, q = lane & 7;
-      const long i0 = tile * 16 + 4 * ray;  // the ray's cell d = L-3
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (i0 < ncells) {
-        const int f = face_of(G, i0);
-        const long at = (long)__float_as_int(med[i0].w) + (long)(q - kGhostD) * normal_step(f, sy, pitch);
-        const float2 a = cur[at], b = prev[at];
-        v = make_float4(a.x, a.y, b.x, b.y);
-      }
-      Ln[warp][ray][q] = v;
-    }
-    __syncwarp();
+  const long tstep = (long)gridDim.x * kInferWarps;
+  // This lane's line point (ray lane/8, point lane%8) and its cell's medium
+  // for a tile, loaded a tile ahead (addresses from the ray index alone).
+  auto load_tile = [&](long tile, float2 &a, float2 &b, float4 &m) {
+    const int ray = lane >> 3, q = lane & 7;
+    const long i0 = tile * 16 + 4 * ray;  // the ray's cell d = L-3
     const long ci = tile * 16 + r;
+    a = b = make_float2(0.f, 0.f);
+    m = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (tile < ntiles && i0 < ncells) {
+      int f;
+      const long at = ghost_index(G, i0, sy, pitch, f) + (long)(q - kGhostD) * normal_step(f, sy, pitch);
+      a = cur[at];
+      b = prev[at];
+    }
+    if (tile < ntiles && ci < ncells) m = med[ci];
+  };
+  long tile = blockIdx.x * (long)kInferWarps + warp;
+  float2 pa, pb;
+  float4 pm;
+  load_tile(tile, pa, pb, pm);
+  for (; tile < ntiles; tile += tstep) {
+    Ln[warp][0][lane >> 3][lane & 7] = pa;
+    Ln[warp][1][lane >> 3][lane & 7] = pb;
+    const long ci = tile * 16 + r;
+    const float4 m = pm;
+    load_tile(tile + tstep, pa, pb, pm);
+    __syncwarp();
     float vv[18];
     float s = 0.f;
-    float4 m = make_float4(0.f, 0.f, 0.f, 0.f);
-    int d = 0;
-    if (ci < ncells) {
-      m = med[ci];
-      const int j = r & 3;  // d = L-3 + j: line points j .. j+8 (past 7: zero)
-      d = G.L - kGhostD + 1 + j;
-      const float4 *line = Ln[warp][r >> 2];
+    const int j = r & 3;  // d = L-3 + j: line points j .. j+8 (past 7: zero)
+    const float2 *line = Ln[warp][half_t][r >> 2];
 #pragma unroll
-      for (int o = 0; o < 9; ++o) {
-        const int q = j + o;
-        const float4 u = q < 8 ? line[q < 8 ? q : 7] : make_float4(0.f, 0.f, 0.f, 0.f);
-        vv[o] = half_t ? u.z : u.x;
-        vv[9 + o] = half_t ? u.w : u.y;
-      }
-#pragma unroll
-      for (int k = 0; k < 18; ++k) s = fmaxf(s, fabsf(vv[k]));
-    } else {
-#pragma unroll
-      for (int k = 0; k < 18; ++k) vv[k] = 0.f;
+    for (int o = 0; o < 9; ++o) {
+      const int q = j + o;
+      const float2 u = (q < 8 && ci < ncells) ? line[q < 8 ? q : 7] : make_float2(0.f, 0.f);
+      vv[o] = u.x;
+      vv[9 + o] = u.y;
     }
+#pragma unroll
+    for (int k = 0; k < 18; ++k) s = fmaxf(s, fabsf(vv[k]));
     s = fmaxf(s, __shfl_xor_sync(0xffffffffu, s, 1));
     // Stencils this small carry no wave (the first cells a front reaches
     // hold values near the FP32 underflow, whose reciprocal overflows).
@@ -493,17 +550,16 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_abc_infer(const __grid_con
     for (int k = 0; k < 18; k += 2)
       *reinterpret_cast<__half2 *>(row + k) = __floats2half2_rn(vv[k] * inv, vv[k + 1] * inv);
     if (half_t == 0) {
-      X[r * kXs + 36] = __float2half_rn(m.x * kVScale);
-      X[r * kXs + 37] = __float2half_rn(m.y);
-      X[r * kXs + 38] = __float2half_rn(m.z);
-      X[r * kXs + 39] = __float2half_rn((float)d / (float)G.L);
+      const int d = G.L - kGhostD + 1 + j;
+      *reinterpret_cast<__half2 *>(X + r * kXs + 36) = __floats2half2_rn(m.x * kVScale, m.y);
+      *reinterpret_cast<__half2 *>(X + r * kXs + 38) = __floats2half2_rn(m.z, (float)d / (float)G.L);
     } else {
 #pragma unroll
-      for (int k = 40; k < kK1; ++k) X[r * kXs + k] = __float2half_rn(0.f);
+      for (int k = 40; k < kK1; k += 2) *reinterpret_cast<__half2 *>(X + r * kXs + k) = __floats2half2_rn(0.f, 0.f);
     }
     __syncwarp();
     float ylo[2], yhi[2];
-    mlp16(X, N, ylo, yhi);
+    mlp16(X, F, ylo, yhi);
     const int g = lane >> 2;
     if ((lane & 3) == 0) {
       const long c0 = tile * 16 + g, c1 = tile * 16 + g + 8;
@@ -518,11 +574,9 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_abc_infer(const __grid_con
 __global__ void __launch_bounds__(32 * kInferWarps) k_abc_forward(const float *feat, long n, const NetHalf *net,
                                                                    float *out) {
   __shared__ __align__(16) __half Xs[kInferWarps][16 * kXs];
-  __shared__ NetHalf N;
-  for (int i = threadIdx.x; i < (int)(sizeof(NetHalf) / 4); i += blockDim.x)
-    reinterpret_cast<uint32_t *>(&N)[i] = reinterpret_cast<const uint32_t *>(net)[i];
-  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Frags F;
+  load_frags(net, F);
   __half *X = Xs[warp];
   const long ntiles = (n + 15) / 16;
   for (long tile = blockIdx.x * (long)kInferWarps + warp; tile < ntiles; tile += (long)gridDim.x * kInferWarps) {
@@ -533,7 +587,7 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_abc_forward(const float *f
     }
     __syncwarp();
     float ylo[2], yhi[2];
-    mlp16(X, N, ylo, yhi);
+    mlp16(X, F, ylo, yhi);
     const int g = lane >> 2;
     if ((lane & 3) == 0) {
       const long c0 = tile * 16 + g, c1 = tile * 16 + g + 8;
@@ -550,78 +604,73 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_abc_forward(const float *f
   }
 }
 
-// The one-way update of the rays of faces f0 and f0 + 1 (one axis), after
+// The one-way update of the rays of the two faces normal to axis A, after
 // the plain step: next[g] = cur[i] + k (cur[g] - next[i]) outward from
 // d = L-3.  Four lanes per ray, one per cell (d = L-3 + lane % 4): each
 // loads its cell's coefficient and current value (the inward one comes from
 // the lane before), the lane of d = L-3 also the inward neighbour's current
-// and next values;
-// the outward dependence next_d = A_d - k_d next_(d-1) (A_d = cur_(d-1) +
-// k_d cur_d) is an inclusive scan of affine maps over the 4 lanes (two
-// shuffle rounds).  The rays of one face are independent.
-__global__ void k_abc_rays(const __grid_constant__ Ghost G, int f0, const float2 *__restrict__ cur,
-                           float2 *__restrict__ next, int sy, int pitch, const float2 *__restrict__ k) {
-  const int rays = (int)((G.off[f0 + 1] - G.off[f0]) / kGhostD);
+// and next values; the outward dependence next_d = A_d - k_d next_(d-1)
+// (A_d = cur_(d-1) + k_d cur_d) is an inclusive scan of affine maps over the
+// 4 lanes (two shuffle rounds).  Grid: x over (first transverse coordinate,
+// lane), y the second transverse coordinate, z the side.  The rays of one
+// face are independent.
+template <int A>
+__global__ void __launch_bounds__(256) k_abc_rays(const __grid_constant__ Ghost G, const float2 *__restrict__ cur,
+                                                  float2 *__restrict__ next, int sy, int pitch,
+                                                  const float2 *__restrict__ k) {
+  constexpr int T0 = A == 0 ? 1 : 0, T1 = A == 2 ? 1 : 2;
+  const int e0 = G.keep.hi[T0] - G.keep.lo[T0];
   const int lane = threadIdx.x & 31, j = lane & 3;
-  // Whole warps step through the rays together (shuffles need every lane).
-  const long nthreads = (long)2 * rays * kGhostD;
-  const long stride = (long)gridDim.x * blockDim.x;
-  for (long t0 = (long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); t0 < nthreads; t0 += stride) {
-    const long t = t0 + lane;
-    const bool live = t < nthreads;
-    const int r = (int)(t / kGhostD);
-    const int f = f0 + (r >= rays ? 1 : 0);
-    const int ray = r - (f - f0) * rays;
-    float2 kk = make_float2(0.f, 0.f), cg = make_float2(0.f, 0.f), ci = make_float2(0.f, 0.f), ni = ci;
-    int gidx = 0;
-    if (live) {
-      const int a = face_axis(f);
-      int t0i, t1i;
-      transverse(a, t0i, t1i);
-      const int e0 = G.keep.hi[t0i] - G.keep.lo[t0i];
-      const int d = G.L - kGhostD + 1 + j;
-      int c[3];
-      c[t0i] = G.keep.lo[t0i] + ray % e0;
-      c[t1i] = G.keep.lo[t1i] + ray / e0;
-      c[a] = face_sign(f) < 0 ? G.in.lo[a] - d : G.in.hi[a] - 1 + d;
-      gidx = (int)cell_index(c[0], c[1], c[2], sy, pitch);
-      kk = k[G.off[f] + (long)ray * kGhostD + j];
-      cg = cur[gidx];
-      if (j == 0) {
-        const int step = normal_step(f, sy, pitch);
-        ci = cur[gidx - step];
-        ni = next[gidx - step];
-      }
-    }
-    // The inward cell of lanes 1 .. 3 is the cell of the lane before.
-    {
-      const float ux = __shfl_up_sync(0xffffffffu, cg.x, 1), uy = __shfl_up_sync(0xffffffffu, cg.y, 1);
-      if (j != 0) ci = make_float2(ux, uy);
-    }
-    // a_d = cur_(d-1) + k_d cur_d, next_d = a_d - k_d next_(d-1): lane j
-    // folds in lanes j-1 .. 0 of its ray (the first one brings next_(L-4)).
-    float ax = __fmaf_rn(kk.x, cg.x, ci.x), ay = __fmaf_rn(kk.y, cg.y, ci.y);
-    float mx = -kk.x, my = -kk.y;  // coefficient of next_(start-1) in the running value
+  const int u = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 2);
+  const int v = blockIdx.y;
+  const int side = blockIdx.z;  // 0: the low face, 1: the high one
+  const int f = 2 * (2 - A) + side;
+  const bool live = u < e0;
+  const int d = G.L - kGhostD + 1 + j;
+  int c[3];
+  c[T0] = G.keep.lo[T0] + u;
+  c[T1] = G.keep.lo[T1] + v;
+  c[A] = side ? G.in.hi[A] - 1 + d : G.in.lo[A] - d;
+  const int stride = A == 0 ? 1 : (A == 1 ? pitch : sy * pitch);
+  const int step = side ? stride : -stride;
+  const int gidx = (c[2] * sy + c[1]) * pitch + c[0];
+  float2 kk = make_float2(0.f, 0.f), cg = kk, ci = kk, ni = kk;
+  if (live) {
+    kk = k[G.off[f] + ((long)v * e0 + u) * kGhostD + j];
+    cg = cur[gidx];
     if (j == 0) {
-      ax = __fmaf_rn(mx, ni.x, ax);
-      ay = __fmaf_rn(my, ni.y, ay);
-      mx = 0.f;
-      my = 0.f;
+      ci = cur[gidx - step];
+      ni = next[gidx - step];
     }
-#pragma unroll
-    for (int o = 1; o < kGhostD; o <<= 1) {
-      const float px = __shfl_up_sync(0xffffffffu, ax, o), py = __shfl_up_sync(0xffffffffu, ay, o);
-      const float qx = __shfl_up_sync(0xffffffffu, mx, o), qy = __shfl_up_sync(0xffffffffu, my, o);
-      if (j >= o) {
-        // value = a + m * (previous value) with the previous one = p + q * (...)
-        ax = __fmaf_rn(mx, px, ax);
-        ay = __fmaf_rn(my, py, ay);
-        mx *= qx;
-        my *= qy;
-      }
-    }
-    if (live) next[gidx] = make_float2(ax, ay);
   }
+  // The inward cell of lanes 1 .. 3 is the cell of the lane before.
+  {
+    const float ux = __shfl_up_sync(0xffffffffu, cg.x, 1), uy = __shfl_up_sync(0xffffffffu, cg.y, 1);
+    if (j != 0) ci = make_float2(ux, uy);
+  }
+  // a_d = cur_(d-1) + k_d cur_d, next_d = a_d - k_d next_(d-1): lane j
+  // folds in lanes j-1 .. 0 of its ray (the first one brings next_(L-4)).
+  float ax = __fmaf_rn(kk.x, cg.x, ci.x), ay = __fmaf_rn(kk.y, cg.y, ci.y);
+  float mx = -kk.x, my = -kk.y;  // coefficient of next_(start-1) in the running value
+  if (j == 0) {
+    ax = __fmaf_rn(mx, ni.x, ax);
+    ay = __fmaf_rn(my, ni.y, ay);
+    mx = 0.f;
+    my = 0.f;
+  }
+#pragma unroll
+  for (int o = 1; o < kGhostD; o <<= 1) {
+    const float px = __shfl_up_sync(0xffffffffu, ax, o), py = __shfl_up_sync(0xffffffffu, ay, o);
+    const float qx = __shfl_up_sync(0xffffffffu, mx, o), qy = __shfl_up_sync(0xffffffffu, my, o);
+    if (j >= o) {
+      // value = a + m * (previous value) with the previous one = p + q * (...)
+      ax = __fmaf_rn(mx, px, ax);
+      ay = __fmaf_rn(my, py, ay);
+      mx *= qx;
+      my *= qy;
+    }
+  }
+  if (live) next[gidx] = make_float2(ax, ay);
 }
 
 // Taper of the layer cells after the step: next *= exp(-(damping d)^2).
@@ -664,9 +713,9 @@ __device__ __forceinline__ float h16(float v) { return __half2float(__float2half
 
 // Forward and backward of B samples (index b of the batch: a random sample,
 // or b itself when seed is 0): loss += sum_c (sigmoid(y_c) a_c - b_c)^2 /
-// (2 B), gradients summed into grad.  Weights are used FP16-rounded,
-// activations are rounded to FP16 between layers (as inference does), the
-// derivatives treat both roundings as the identity.  noise > 0 perturbs the
+// (2 B), gradients summed into grad.  Weights are used FP16-rounded, hidden
+// pre-activations and activations are rounded to FP16 (as inference does),
+// the derivatives treat the roundings as the identity.  noise > 0 perturbs the
 // stencil inputs.
 __global__ void __launch_bounds__(kTB) k_abc_train(const float *feat, const float *tgt, long nsamp, int B,
                                                     uint32_t seed, const float *P, float noise, float *grad,
@@ -704,13 +753,13 @@ __global__ void __launch_bounds__(kTB) k_abc_train(const float *feat, const floa
   for (int o = 0; o < kHid; ++o) {
     float z = b1[o];
     for (int k = 0; k < kIn; ++k) z = fmaf(W1[o * kIn + k], x[k], z);
-    a1[o] = tanhf(z);
+    a1[o] = tanhf(h16(z));  // inference rounds the pre-activation to FP16 for its half2 tanh
     h1[o] = live ? h16(a1[o]) : 0.f;
   }
   for (int o = 0; o < kHid; ++o) {
     float z = b2[o];
     for (int k = 0; k < kHid; ++k) z = fmaf(W2[o * kHid + k], h1[k], z);
-    a2[o] = tanhf(z);
+    a2[o] = tanhf(h16(z));
     h2[o] = live ? h16(a2[o]) : 0.f;
   }
   float l = 0.f;
@@ -906,7 +955,7 @@ cudaError_t abc_before_step(const ResidentView &v) {
   if (R.steps++ % R.interval != 0) return cudaSuccess;  // the last coefficients stay
   const long ntiles = (R.G.off[6] + 15) / 16;
   const long grid = (ntiles + kInferWarps - 1) / kInferWarps;
-  const long cap = v.num_sms > 0 ? (long)v.num_sms * 8 : 1024;
+  const long cap = v.num_sms > 0 ? (long)v.num_sms * kInferBlocksPerSm : 1024;
   k_abc_infer<<<(int)(grid < cap ? grid : cap), 32 * kInferWarps, 0, v.stream>>>(R.G, v.cur, v.prev, v.sy, v.pitch,
                                                                                  R.med, T.net, R.k);
   return cudaGetLastError();
@@ -915,10 +964,15 @@ cudaError_t abc_before_step(const ResidentView &v) {
 cudaError_t abc_after_step(const ResidentView &v) {
   if (!R.on) return cudaSuccess;
   if (oneway_mode(R.mode)) {
-    for (int f0 = 0; f0 < 6; f0 += 2) {  // z faces, y faces, x faces
-      const long threads = 2 * (R.G.off[f0 + 1] - R.G.off[f0]);  // one per ghost cell of the two faces
-      k_abc_rays<<<grid_of(threads, 256), 256, 0, v.stream>>>(R.G, f0, v.cur, v.next, v.sy, v.pitch, R.k);
-    }
+    // z faces, then y faces, then x faces (edge and corner cells keep the last value).
+    auto grid = [&](int a) {
+      const int t0 = a == 0 ? 1 : 0, t1 = a == 2 ? 1 : 2;
+      const int e0 = R.G.keep.hi[t0] - R.G.keep.lo[t0], e1 = R.G.keep.hi[t1] - R.G.keep.lo[t1];
+      return dim3((unsigned)((e0 * kGhostD + 255) / 256), (unsigned)e1, 2u);
+    };
+    k_abc_rays<2><<<grid(2), 256, 0, v.stream>>>(R.G, v.cur, v.next, v.sy, v.pitch, R.k);
+    k_abc_rays<1><<<grid(1), 256, 0, v.stream>>>(R.G, v.cur, v.next, v.sy, v.pitch, R.k);
+    k_abc_rays<0><<<grid(0), 256, 0, v.stream>>>(R.G, v.cur, v.next, v.sy, v.pitch, R.k);
   }
   if (R.damping > 0.f && R.ncells)
     k_abc_taper<<<grid_of(R.ncells, 256), 256, 0, v.stream>>>(R.cells, R.ncells, v.next, v.sy, v.pitch, R.damping);

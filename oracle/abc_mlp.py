@@ -5,8 +5,9 @@ fletcher_petrobras_gb300/csrc/abc_learned.cu, used by the tests to check the
 GPU kernels:
 
 * `forward` / `loss_and_grad`: the 40 -> 32 -> 32 -> 2 tanh network with the
-  same roundings as the GPU path (weights, inputs and hidden activations
-  rounded to FP16, biases and accumulation unrounded), the loss
+  same roundings as the GPU path (weights, inputs, hidden pre-activations
+  and activations rounded to FP16, biases and accumulation unrounded), the
+  loss
   sum_c (sigmoid(y_c) a_c - b_c)^2 / (2 n) and its analytic gradient
   (roundings treated as the identity);
 * `ghost_cells`: the ghost zone's cells in the library's order (faces z-,
@@ -56,9 +57,9 @@ def forward(P, X, rounding=True):
     w = unpack(P)
     W1, W2, W3 = (_h16(w[k], rounding) for k in ("W1", "W2", "W3"))
     x = _h16(X, rounding)
-    a1 = np.tanh(x @ W1.T + w["b1"])
+    a1 = np.tanh(_h16(x @ W1.T + w["b1"], rounding))
     h1 = _h16(a1, rounding)
-    a2 = np.tanh(h1 @ W2.T + w["b2"])
+    a2 = np.tanh(_h16(h1 @ W2.T + w["b2"], rounding))
     h2 = _h16(a2, rounding)
     y = h2 @ W3.T + w["b3"]
     return y, dict(x=x, a1=a1, h1=h1, a2=a2, h2=h2, W2=W2, W3=W3)
