@@ -51,9 +51,11 @@ struct State {
   ShotDesc desc;                 // the shot (passed by value to every launch)
   ShotMaps maps;                 // its TMA descriptors
   int tile_rows = 12, stages = 5, zchunks = 0;
-  int grid = 0, nitems = 0, ntx = 0, nty = 0;
-  int4 *seg = nullptr;     // single-shot work segments {x0, y0, z0, z1}
-  int *cta_first = nullptr;  // [grid + 1]: first segment of each CTA
+  int grid = 0, nitems = 0, ntx = 0, nty = 0, chunk = 0;  // the FP32 launch's items
+  bool spread = false;       // the plan shares out its last round (segment list launch)
+  int4 *seg = nullptr;       // the plan as work segments {x0, y0, z0, z1}
+  int *cta_first = nullptr;  // [seg_grid + 1]: first segment of each CTA
+  int nseg = 0, seg_grid = 0;
   long launches = 0;
   size_t dev_bytes = 0;
   int num_sms = 0;
@@ -295,6 +297,8 @@ struct Split {
   std::vector<int4> seg;
   std::vector<int> first;
   long max_cost = 0, total_cost = 0;
+  bool spread = false;  // false: uniform chunks of `len` planes, all round-robin
+  int len = 0;
 };
 
 Split split_work(int ctas, int ntx, int nty, int TY, int zlo, int depth, int nchunk, bool spread = true) {
@@ -338,6 +342,8 @@ Split split_work(int ctas, int ntx, int nty, int TY, int zlo, int depth, int nch
     }
   }
   Split sp;
+  sp.spread = full < items;
+  sp.len = len;
   sp.first.push_back(0);
   for (int b = 0; b < ctas; ++b) {
     sp.seg.insert(sp.seg.end(), per[b].begin(), per[b].end());
@@ -507,16 +513,28 @@ int setup_tiles(int rows, int stages) {
   CK(cudaMalloc(&g.cta_first, sp.first.size() * sizeof(int)));
   CK(cudaMemcpy(g.seg, sp.seg.data(), sp.seg.size() * sizeof(int4), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(g.cta_first, sp.first.data(), sp.first.size() * sizeof(int), cudaMemcpyHostToDevice));
-  g.nitems = (int)sp.seg.size();
   // CTAs past the last one with work are not launched.
   int grid = ctas;
   while (grid > 1 && sp.first[grid - 1] == sp.first[grid]) --grid;
-  g.grid = grid;
+  g.seg_grid = grid;
+  g.nseg = (int)sp.seg.size();
+  g.spread = sp.spread;
+  if (sp.spread) {
+    g.nitems = g.nseg;
+    g.grid = grid;
+    g.chunk = 0;
+  } else {
+    // A round-robin plan: the FP32 kernel decodes its items arithmetically
+    // (tiles x chunks of `len` planes, chunk-major), no list lookups.
+    g.chunk = sp.len;
+    g.nitems = g.ntx * g.nty * ((sz - 2 * bord + sp.len - 1) / sp.len);
+    g.grid = std::min(g.nitems, ctas);
+  }
   memset(&g.desc, 0, sizeof(g.desc));
   g.desc.F[0] = g.F[0];
   g.desc.F[1] = g.F[1];
   g.desc.sx = sx; g.desc.sy = sy; g.desc.sz = sz; g.desc.pitch = g.pitch; g.desc.bord = bord;
-  g.desc.ntx = g.ntx; g.desc.nty = g.nty;
+  g.desc.ntx = g.ntx; g.desc.nty = g.nty; g.desc.chunk = g.chunk;
   g.desc.src_x = g.desc.src_y = g.desc.src_z = -1000;
   g.desc.cor_x = g.desc.cor_y = g.desc.cor_z = -1000;
   return FLETCHER_OK;
@@ -711,7 +729,7 @@ int step() {
   P.shots = nullptr;
   P.maps = nullptr;
   P.items = nullptr;
-  P.seg = g.seg;
+  P.seg = g.spread ? g.seg : nullptr;
   P.cta_first = g.cta_first;
   P.nitems = g.nitems;
   P.parity = c;
@@ -763,6 +781,8 @@ int step() {
     CK(half_scales(g.Mx + c * sz, g.Mx + p * sz, g.E + enew * sz, sz, sz_src, sabs, g_stream));
     HalfLaunch HL;
     HL.h.p = P;
+    HL.h.p.seg = g.seg;  // the 16-bit kernel always walks the segment list
+    HL.h.p.nitems = g.nseg;
     HL.h.out_hi = g.Hh[p];
     HL.h.out_lo = g.Hl[p];
     HL.h.e_cur = g.E + g.ecur * sz;
@@ -772,7 +792,7 @@ int step() {
     HL.m = g.hm[c];
     HL.tile_rows = g.tile_rows;
     HL.stages = g.stages;
-    HL.grid = g.grid;
+    HL.grid = g.seg_grid;
     CK(propagate_half_launch(HL, g.form == FLETCHER_FORM_FP16X, g_stream));
     g.ecur = enew;
   } else {

@@ -43,15 +43,15 @@ struct alignas(64) ShotMaps {
 // One launch: every active shot advances one step.
 //  * batched launches: work items {shot, x0, y0, chunk index}, ordered by
 //    shot; CTA b takes items b, b + grid, ... below nitems;
-//  * single-shot launches: segments {x0, y0, z0, z1} (a z range of one tile
-//    column); CTA b takes segments cta_first[b] .. cta_first[b + 1] - 1.
+//  * single-shot launches with seg: segments {x0, y0, z0, z1} (a z range of
+//    one tile column); CTA b takes segments cta_first[b] .. cta_first[b+1]-1;
+//  * single-shot launches without seg: items = tiles x uniform z-chunks of
+//    one.chunk planes, chunk-major, CTA b takes b, b + grid, ... below nitems.
 struct PropParams {
   ShotDesc one;                     // single-shot launches: the shot itself
   const ShotDesc *shots;            // batched launches: per-shot descriptors
   const ShotMaps *maps;
   const int4 *items;                // batched launches
-  const int4 *seg;                  // single-shot launches
-  const int *cta_first;             // single-shot launches: [grid + 1]
   int nitems;
   int parity;                       // current field = F[parity], previous = F[1 - parity]
   float inv_dx, inv_dy, inv_dz;     // 1/dx, 1/dy, 1/dz
@@ -61,6 +61,8 @@ struct PropParams {
   float src;                        // value added at each shot's source cell (src_z >= 0)
   float cor;                        // value owed at each shot's cor cell (cor_z >= 0)
   unsigned int *err;                // error word (bit 0: bounded wait gave up)
+  const int4 *seg;                  // single-shot launches with a segment list
+  const int *cta_first;             // their [grid + 1] first segments
 };
 
 // The four descriptors a single-shot launch passes as kernel parameters.

@@ -70,10 +70,18 @@ struct Item {
   int shot;
 };
 
-template <int TY, bool BATCH>
+// Work-item kinds of a launch (template parameter MODE):
+//  * kItemsTiles: single shot, items = tiles x uniform z-chunks, chunk-major,
+//    CTA b takes b, b + grid, ... (decoded arithmetically, no lookups);
+//  * kItemsBatch: batched shots, P.items {shot, x0, y0, chunk}, same order;
+//  * kItemsSegments: single shot, P.seg {x0, y0, z0, z1}, CTA b takes its run
+//    cta_first[b] .. cta_first[b + 1] - 1.
+constexpr int kItemsTiles = 0, kItemsBatch = 1, kItemsSegments = 2;
+
+template <int TY, int MODE>
 __device__ __forceinline__ Item decode_item(int item, const PropParams &P) {
   Item it;
-  if constexpr (BATCH) {
+  if constexpr (MODE == kItemsBatch) {
     const int4 w = P.items[item];  // {shot, x0, y0, chunk index}
     const ShotDesc &d = P.shots[w.x];
     it.x0 = w.y;
@@ -81,12 +89,23 @@ __device__ __forceinline__ Item decode_item(int item, const PropParams &P) {
     it.z0 = d.bord + w.w * d.chunk;
     it.z1 = min(it.z0 + d.chunk, d.sz - d.bord);
     it.shot = w.x;
-  } else {
+  } else if constexpr (MODE == kItemsSegments) {
     const int4 w = P.seg[item];  // {x0, y0, z0, z1}
     it.x0 = w.x;
     it.y0 = w.y;
     it.z0 = w.z;
     it.z1 = w.w;
+    it.shot = 0;
+  } else {
+    const ShotDesc &d = P.one;
+    const int tx = item % d.ntx;
+    const int r = item / d.ntx;
+    const int ty = r % d.nty;
+    const int ch = r / d.nty;
+    it.x0 = kRadius + tx * kTileX;
+    it.y0 = kRadius + ty * TY;
+    it.z0 = d.bord + ch * d.chunk;
+    it.z1 = min(it.z0 + d.chunk, d.sz - d.bord);
     it.shot = 0;
   }
   return it;
@@ -96,10 +115,10 @@ __device__ __forceinline__ Item decode_item(int item, const PropParams &P) {
 struct ItemRange {
   int first, end, step;
 };
-template <bool BATCH>
+template <int MODE>
 __device__ __forceinline__ ItemRange item_range(const PropParams &P) {
-  if constexpr (BATCH) return {(int)blockIdx.x, P.nitems, (int)gridDim.x};
-  else return {P.cta_first[blockIdx.x], P.cta_first[blockIdx.x + 1], 1};
+  if constexpr (MODE == kItemsSegments) return {P.cta_first[blockIdx.x], P.cta_first[blockIdx.x + 1], 1};
+  else return {(int)blockIdx.x, P.nitems, (int)gridDim.x};
 }
 
 // Descriptors used for one step of item `it`.
@@ -131,9 +150,10 @@ __device__ __forceinline__ void issue_step(unsigned char *stage, uint64_t *bar, 
   }
 }
 
-template <int TY, int S, bool ISO, bool BATCH, int MINB>
+template <int TY, int S, bool ISO, int MODE, int MINB>
 __global__ void __launch_bounds__(kTileX *TY, MINB)
     k_propagate_fp32(const __grid_constant__ SingleMaps SM, const __grid_constant__ PropParams P) {
+  constexpr bool BATCH = MODE == kItemsBatch;
   using G = Geo<TY>;
   extern __shared__ unsigned char smem_dyn[];
   // Align in the shared window (pointer arithmetic on the shared array keeps
@@ -149,8 +169,13 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   const int lx = tid & 31;
   const int ly = tid >> 5;
 
-  const ItemRange R = item_range<BATCH>(P);
+  // This CTA's items.  A segment run's end lives in shared memory (read once
+  // per item), so the loop keeps no register for it.
+  const ItemRange R = item_range<MODE>(P);
   if (R.first >= R.end) return;
+  volatile int *s_end = s_abort + 1;
+  auto item_end = [&]() { return MODE == kItemsSegments ? *s_end : P.nitems; };
+  auto item_step = [&]() { return MODE == kItemsSegments ? 1 : (int)gridDim.x; };
   // The producer is lane 0 of the last warp (warps 0 .. TY/4-1 carry the
   // halo-column work).  Its cursor, in shared memory, is the next step to load.
   const bool producer = tid == (TY - 1) * 32;
@@ -177,9 +202,9 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
     issue_step<TY>(smem + c.stage * G::STAGE_B, &full[c.stage], c.it, c.k, maps_of(c.it));
     if (++c.stage == S) c.stage = 0;
     if (++c.k >= c.it.z1 + kRadius) {
-      c.item += R.step;
-      if (c.item < R.end) {
-        c.it = decode_item<TY, BATCH>(c.item, P);
+      c.item += item_step();
+      if (c.item < item_end()) {
+        c.it = decode_item<TY, MODE>(c.item, P);
         c.k = c.it.z0 - kRadius;
       }
     }
@@ -190,10 +215,11 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
     mbar_init(xchg, TY);
     mbar_fence_init();
     *s_abort = 0;
+    if constexpr (MODE == kItemsSegments) *s_end = R.end;
   }
   if (producer) {
     Cursor c;
-    c.it = decode_item<TY, BATCH>(R.first, P);
+    c.it = decode_item<TY, MODE>(R.first, P);
     c.item = R.first;
     c.k = c.it.z0 - kRadius;
     c.stage = 0;
@@ -209,7 +235,7 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
       tma_prefetch_desc(m.upd);
     }
     // Prologue: the first S-2 steps of this CTA.
-    for (int a = 0; a < S - 2 && cur->item < R.end; ++a) produce();
+    for (int a = 0; a < S - 2 && cur->item < item_end(); ++a) produce();
   }
 
   // Spacing factors (unused on isotropic grids).
@@ -226,8 +252,8 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   uint32_t phase = 0, xphase = 0;
   int dsel = 0;
   int abw = 0;  // shared A/B ring slot of the arriving plane (the plane 4 back is at abw + 1)
-  for (int item = R.first; item < R.end; item += R.step) {
-    const Item it = decode_item<TY, BATCH>(item, P);
+  for (int item = R.first; item < item_end(); item += item_step()) {
+    const Item it = decode_item<TY, MODE>(item, P);
     const ShotDesc &sd = BATCH ? P.shots[it.shot] : P.one;
     const int kbeg = it.z0 - kRadius;
     const int kend = it.z1 + kRadius;
@@ -315,7 +341,7 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
         // The producer has passed the exchange of the previous step, so every
         // thread is past the step before it: refill that step's stage with
         // the next step due (S-2 steps ahead of this one).
-        if (producer && cur->item < R.end) {
+        if (producer && cur->item < item_end()) {
           fence_proxy_async_smem();
           produce();
         }
@@ -410,8 +436,10 @@ template <int TY, int S, int MINB>
 static cudaError_t prepare_t() {
   constexpr size_t smem = smem_bytes<TY, S>();
   cudaError_t e = cudaSuccess;
-  for (auto kern : {k_propagate_fp32<TY, S, true, true, MINB>, k_propagate_fp32<TY, S, false, true, MINB>,
-                    k_propagate_fp32<TY, S, true, false, MINB>, k_propagate_fp32<TY, S, false, false, MINB>})
+  for (auto kern : {k_propagate_fp32<TY, S, true, kItemsTiles, MINB>, k_propagate_fp32<TY, S, false, kItemsTiles, MINB>,
+                    k_propagate_fp32<TY, S, true, kItemsBatch, MINB>, k_propagate_fp32<TY, S, false, kItemsBatch, MINB>,
+                    k_propagate_fp32<TY, S, true, kItemsSegments, MINB>,
+                    k_propagate_fp32<TY, S, false, kItemsSegments, MINB>})
     if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   return e;
 }
@@ -426,8 +454,12 @@ static cudaError_t launch_t(const PropLaunch &L, cudaStream_t s) {
     ready = true;
   }
   const bool iso = L.p.iso != 0;
-  auto kern = L.batch ? (iso ? k_propagate_fp32<TY, S, true, true, MINB> : k_propagate_fp32<TY, S, false, true, MINB>)
-                      : (iso ? k_propagate_fp32<TY, S, true, false, MINB> : k_propagate_fp32<TY, S, false, false, MINB>);
+  auto kern = L.batch      ? (iso ? k_propagate_fp32<TY, S, true, kItemsBatch, MINB>
+                                  : k_propagate_fp32<TY, S, false, kItemsBatch, MINB>)
+              : L.p.seg    ? (iso ? k_propagate_fp32<TY, S, true, kItemsSegments, MINB>
+                                  : k_propagate_fp32<TY, S, false, kItemsSegments, MINB>)
+                           : (iso ? k_propagate_fp32<TY, S, true, kItemsTiles, MINB>
+                                  : k_propagate_fp32<TY, S, false, kItemsTiles, MINB>);
   kern<<<L.grid, kTileX * TY, smem, s>>>(L.m, L.p);
   return cudaGetLastError();
 }
