@@ -554,11 +554,11 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
     return fail(FLETCHER_ERR_ARGS, "unknown storage form %d", g_form);
   const bool half = g_form != FLETCHER_FORM_FP32;
   const bool ext = g_form == FLETCHER_FORM_FP16X;
-  // Default shapes (measured at 504^3): 16 rows; 5 stages (FP32 2.20 ms per
-  // step against 2.40 for 12 x 5; FP16 3.21 against 3.56), 4 for FP16X (3.74
-  // against 4.13 for 12 x 5).
+  // Default shapes (measured at 504^3): 16 rows; 5 stages for FP32 (2.20 ms
+  // per step against 2.40 for 12 x 5) and FP16X (3.45 against 3.68 for 16 x 4),
+  // 4 for FP16 (3.02 against 3.18 for 16 x 5).
   const int rows = g_req_rows ? g_req_rows : 16;
-  const int stages = g_req_stages ? g_req_stages : (ext ? 4 : 5);
+  const int stages = g_req_stages ? g_req_stages : (g_form == FLETCHER_FORM_FP16 ? 4 : 5);
   if (!(half ? propagate_half_supported(rows, stages) : propagate_fp32_supported(rows, stages)))
     return fail(FLETCHER_ERR_ARGS, "tile shape (%d rows, %d stages) is not built for form %d", rows, stages, g_form);
   if (half) {

@@ -16,7 +16,8 @@
 // an FP32 shared-memory tile once per cell, then runs the FP32 stencil of
 // propagate_fp32.cu on it.  The updated plane is encoded with its new scale,
 // and the CTA's largest magnitude on it is folded (atomicMax) into the
-// per-plane maximum that the next step's scales use.
+// per-plane maximum that the next step's scales use; a magnitude beyond
+// FP16's range there sets bit 2 of the error word.
 #include <cuda_fp16.h>
 
 #include "device_util.cuh"
@@ -166,14 +167,18 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
   uint64_t *xchg = full + S;
   int *ctl = reinterpret_cast<int *>(xchg + 1);
   int *cur = ctl;                                          // producer cursor: item, k, stage
+  volatile int *s_end = ctl + 3;                           // end of this CTA's segments
   unsigned *smax = reinterpret_cast<unsigned *>(ctl + 4);  // CTA max of the plane updated, by step parity
+  volatile int *s_pend = ctl + 6;  // plane whose CTA maximum waits in smax[sel ^ 1] (-1: none)
 
   const int tid = threadIdx.x;
   const int lx = tid & 31;
   const int ly = tid >> 5;
-  // This CTA's segments: cta_first[b] .. cta_first[b + 1] - 1.
-  const int item_first = P.cta_first[blockIdx.x], item_end = P.cta_first[blockIdx.x + 1];
-  if (item_first >= item_end) return;
+  // This CTA's segments: cta_first[b] .. cta_first[b + 1] - 1.  The end
+  // and thread 0's pending plane live in shared memory (no loop registers).
+  const int item_first = P.cta_first[blockIdx.x];
+  if (item_first >= P.cta_first[blockIdx.x + 1]) return;
+  auto item_end = [&]() { return *s_end; };
   const bool producer = tid == (TY - 1) * 32;
   auto produce = [&]() {
     int item = cur[0], k = cur[1], stg = cur[2];
@@ -182,7 +187,7 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
     if (++stg == S) stg = 0;
     if (++k >= it.z1 + kRadius) {
       ++item;
-      if (item < item_end) k = decode_hitem(item, P).z0 - kRadius;
+      if (item < item_end()) k = decode_hitem(item, P).z0 - kRadius;
     }
     cur[0] = item;
     cur[1] = k;
@@ -195,6 +200,8 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
     cur[0] = item_first;
     cur[1] = decode_hitem(item_first, P).z0 - kRadius;
     cur[2] = 0;
+    *s_end = P.cta_first[blockIdx.x + 1];
+    *s_pend = -1;
     smax[0] = smax[1] = 0u;
   }
   __syncthreads();
@@ -205,7 +212,7 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
     tma_prefetch_desc(&M.upd);
     // Prologue: S-1 steps; afterwards each step refills the stage freed by
     // the step before it.
-    for (int a = 0; a < S - 1 && cur[0] < item_end; ++a) produce();
+    for (int a = 0; a < S - 1 && cur[0] < item_end(); ++a) produce();
   }
 
   const float sx1 = P.inv_dx, sy1 = P.inv_dy, sz1 = P.inv_dz;
@@ -220,9 +227,8 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
   uint32_t phase = 0, xphase = 0;
   int sel = 0;
   int abw = 0;  // shared A/B ring slot of the arriving plane (the plane 4 back is at abw + 1)
-  int pend_z = -1;  // thread 0: plane whose CTA maximum waits in smax[sel ^ 1]
   bool bad = false;
-  for (int item = item_first; item < item_end; ++item) {
+  for (int item = item_first; item < item_end(); ++item) {
     const HItem it = decode_hitem(item, P);
     const int kbeg = it.z0 - kRadius;
     const int kend = it.z1 + kRadius;
@@ -233,12 +239,6 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
     const int ci = ly * G::TX + lx;
     const int hc = (ly + kRadius) * G::HX + (lx + kRadius);
     const int src_z = sd.src_z, cor_z = sd.cor_z;
-    // Halo-tile index of the source cell (-1: not in this tile).
-    int src_c = -1;
-    {
-      const int rx = sd.src_x - (it.x0 - kRadius), ry = sd.src_y - (it.y0 - kRadius);
-      if (rx >= 0 && rx < G::HX && ry >= 0 && ry < G::HY) src_c = ry * G::HX + rx;
-    }
 
     f2 Pr[9], Dx[9], Dy[9], A[9], B[9];
 
@@ -251,21 +251,32 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
         bad |= !mbar_wait(&full[stage], phase, kWaitLimitNs);
         f2 *Hs = H32 + sel * G::HXY;
         {
-          // Decode the arriving plane once per cell; the source cell gains
-          // the step's source (original/OpenMP/openmp_insertsource.c:7-13).
-          // Threads take cells from the last one down, so the remainder falls
-          // to the last warps, which carry no halo-column work.
+          // Decode the arriving plane once per cell, two cells per thread
+          // (one 64-bit load of two half2 cells, one 128-bit store of their
+          // FP32 pairs).  The source cell then gains the step's source
+          // (original/OpenMP/openmp_insertsource.c:7-13), added by the
+          // thread that decoded it.
           const float inv = exp2i(-H.e_cur[k]);
-          const int sc = (k == src_z) ? src_c : -1;
-          const unsigned *hv = reinterpret_cast<const unsigned *>(st);
-          const unsigned short *rv = reinterpret_cast<const unsigned short *>(st + G::OFF_LO);
+          const uint2 *hv2 = reinterpret_cast<const uint2 *>(st);
+          const unsigned *rv2 = reinterpret_cast<const unsigned *>(st + G::OFF_LO);
+          float4 *Hs4 = reinterpret_cast<float4 *>(Hs);
 #pragma unroll
-          for (int c0 = 0; c0 < G::HXY; c0 += NTH) {
-            const int c = c0 + (NTH - 1 - tid);
-            if (c < G::HXY) {
-              f2 v = decode<EXT>(hv[c], EXT ? rv[c] : (unsigned short)0, inv);
-              if (c == sc) v = add2(v, splat(P.src));
-              Hs[c] = v;
+          for (int c0 = 0; c0 < G::HXY / 2; c0 += NTH) {
+            const int c2 = c0 + tid;
+            if (c2 < G::HXY / 2) {
+              const uint2 h = hv2[c2];
+              const unsigned r = EXT ? rv2[c2] : 0u;
+              const f2 a = decode<EXT>(h.x, (unsigned short)(r & 0xffffu), inv);
+              const f2 b = decode<EXT>(h.y, (unsigned short)(r >> 16), inv);
+              Hs4[c2] = make_float4(lo(a), hi(a), lo(b), hi(b));
+            }
+          }
+          if (k == src_z) {
+            // Halo-tile index of the source cell, if it lies in this tile.
+            const int rx = sd.src_x - (it.x0 - kRadius), ry = sd.src_y - (it.y0 - kRadius);
+            if (rx >= 0 && rx < G::HX && ry >= 0 && ry < G::HY) {
+              const int src_c = ry * G::HX + rx;
+              if (tid == (src_c >> 1) % NTH) Hs[src_c] = add2(Hs[src_c], splat(P.src));
             }
           }
         }
@@ -273,18 +284,23 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
         // CTA maximum of the plane it updated is complete.  Every thread
         // takes the same branch (a wait that gave up anywhere ends the CTA).
         if (__syncthreads_or(bad)) goto aborted;
-        if (producer && cur[0] < item_end) {
+        if (producer && cur[0] < item_end()) {
           fence_proxy_async_smem();
           produce();
         }
-        if (tid == 0 && pend_z >= 0) {
+        if (tid == 0 && *s_pend >= 0) {
+          const int pend_z = *s_pend;
           const unsigned v = smax[sel ^ 1];
           smax[sel ^ 1] = 0u;
-          if (v) atomicMax(&H.m_new[pend_z], v);
+          if (v) {
+            atomicMax(&H.m_new[pend_z], v);
+            // Beyond FP16's range: the scale bound was exceeded.
+            if (!(__fmul_rn(__uint_as_float(v), exp2i(H.e_new[pend_z])) < 65504.0f)) atomicOr(P.err, 4u);
+          }
         }
         const bool center = (k >= it.z0) && (k < it.z1);
         const bool upd = (k - kRadius >= it.z0);
-        if (tid == 0) pend_z = upd ? k - kRadius : -1;
+        if (tid == 0) *s_pend = upd ? k - kRadius : -1;
 
         const f2 c = Hs[hc];
         f2 xa[4], xb[4], ya[4], yb[4];
@@ -366,14 +382,13 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
             H.out_hi[(long)zc * plane + oidx] = ohv;
             if constexpr (EXT) H.out_lo[(long)zc * plane + oidx] = orv;
           }
-          float m = valid ? fmaxf(fabsf(lo(nw)), fabsf(hi(nw))) : 0.0f;
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-          if (lx == 0 && m > 0.0f) {
-            atomicMax(&smax[sel], __float_as_uint(m));
-            // Beyond FP16's range: the scale bound was exceeded.
-            if (!(__fmul_rn(m, scl) < 65504.0f)) atomicOr(P.err, 4u);
-          }
+          // The warp's largest magnitude: the bits of non-negative floats
+          // order like the floats, so one integer warp reduction finds it
+          // (a NaN, above every finite value, reaches the range check).
+          unsigned mb = 0u;
+          if (valid) mb = max(__float_as_uint(fabsf(lo(nw))), __float_as_uint(fabsf(hi(nw))));
+          mb = __reduce_max_sync(0xffffffffu, mb);
+          if (lx == 0 && mb) atomicMax(&smax[sel], mb);
         }
         bad |= !mbar_wait(xchg, xphase, kWaitLimitNs);
         xphase ^= 1u;
@@ -402,9 +417,13 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
   }
   // The last plane's CTA maximum.
   if (__syncthreads_or(bad)) goto aborted;
-  if (tid == 0 && pend_z >= 0) {
+  if (tid == 0 && *s_pend >= 0) {
+    const int pend_z = *s_pend;
     const unsigned v = smax[sel ^ 1];
-    if (v) atomicMax(&H.m_new[pend_z], v);
+    if (v) {
+      atomicMax(&H.m_new[pend_z], v);
+      if (!(__fmul_rn(__uint_as_float(v), exp2i(H.e_new[pend_z])) < 65504.0f)) atomicOr(P.err, 4u);
+    }
   }
   return;
 aborted:
