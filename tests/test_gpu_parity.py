@@ -120,9 +120,13 @@ def test_previous_fields_match_oracle(orc):
     assert abs(pp[i] - opp[i]) <= 1e-5 * np.abs(opp).max()
 
 
-@pytest.mark.parametrize("tile", [(12, 4, 1), (12, 4, 3), (16, 5, 2), (16, 4, 0), (8, 5, 5), (12, 5, 0), (12, 6, 0), (8, 5, 2)])
+@pytest.mark.parametrize("tile", [(12, 4, 1), (12, 4, 3), (16, 5, 2), (16, 4, 0), (8, 5, 5), (12, 5, 0), (12, 6, 0),
+                                  (8, 5, 2), (16, 5, -1), (12, 4, -3)])
 def test_tile_shapes_bit_identical(tile, orc):
-    """Every tile shape, stage count and z-chunking computes identical floats."""
+    """Every tile shape, stage count and z-chunking computes identical floats,
+    through both work-item modes: segment lists (zchunks >= 0 here: the
+    small grid has fewer items than CTAs, so the plan shares them out) and
+    arithmetic round-robin items (zchunks < 0)."""
     prob = Problem("shapes", 70, 27, 33, absorb=5, dt=0.0006, steps=24, fcut=45.0, kind="layered", layers=5,
                    seed=9)
     prob = prob.with_(source=(prob.sx // 2 + 1, prob.sy // 2, prob.sz // 2 + 2))
