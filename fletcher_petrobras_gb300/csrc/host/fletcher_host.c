@@ -214,18 +214,31 @@ int FLETCHER_Model(int st, long iSource, double fcut, float dt_output, int sx, i
     }
   }
   FLETCHER_SnapshotWait();
+  if (FLETCHER_GetLastError()) {
+    const int e = FLETCHER_GetLastError();
+    if (pinned) {
+      FLETCHER_UnpinHost(pp);
+      FLETCHER_UnpinHost(pc);
+    }
+    DRIVER_Finalize();
+    return e;
+  }
+  /* The final p and q go into page-locked destinations too (the copy
+   * engine writes them at full speed; into pageable memory the copy is
+   * staged by the driver, and memory the caller never touched is faulted
+   * in during it).  pc0 is one of the two p arrays. */
+  const int pin_p = !pinned && !FLETCHER_PinHost(pc0, n * sizeof(float));
+  const int pin_q = !FLETCHER_PinHost(qc0, n * sizeof(float));
+  FLETCHER_ClearError(); /* a destination that could not be locked is copied to as it is */
+  int rc = FLETCHER_GetField(0, pc0);
+  if (!rc) rc = FLETCHER_GetField(1, qc0);
+  d2h += 2.0 * n * sizeof(float);
+  if (pin_q) FLETCHER_UnpinHost(qc0);
+  if (pin_p) FLETCHER_UnpinHost(pc0);
   if (pinned) {
     FLETCHER_UnpinHost(pp);
     FLETCHER_UnpinHost(pc);
   }
-  if (FLETCHER_GetLastError()) {
-    const int e = FLETCHER_GetLastError();
-    DRIVER_Finalize();
-    return e;
-  }
-  int rc = FLETCHER_GetField(0, pc0);
-  if (!rc) rc = FLETCHER_GetField(1, qc0);
-  d2h += 2.0 * n * sizeof(float);
   DRIVER_Finalize();
   const double t_end = wall_seconds();
   if (stats) {
