@@ -104,3 +104,20 @@ def test_oneway_update_transports_a_plane_wave():
     flat = np.ones((2, S, S, S))
     out = abc_mlp.oneway_update(flat, flat.copy(), lo, hi, L, kk)
     assert np.allclose(out, 1.0)
+
+
+def test_boundary_arguments_are_checked_on_the_host(lib):
+    """Host-side checks of part 4, before any CUDA call: the network interval
+    must be positive, a boundary needs an initialised state, an unknown mode
+    is refused."""
+    lib.FLETCHER_SetErrorMode(1)
+    lib.FLETCHER_ClearError()
+    assert lib.FLETCHER_AbcSetInterval(0) != 0
+    lib.FLETCHER_ClearError()
+    assert lib.FLETCHER_AbcSetInterval(3) == 0
+    assert lib.FLETCHER_AbcSetInterval(1) == 0
+    assert lib.FLETCHER_SetBoundary(1, 8, 0.0) != 0  # no DRIVER_Initialize yet
+    lib.FLETCHER_ClearError()
+    assert lib.FLETCHER_SetBoundary(7, 8, 0.0) != 0
+    lib.FLETCHER_ClearError()
+    assert lib.FLETCHER_AbcLayerCells() == 0
