@@ -38,7 +38,9 @@
 //     layer-2 outputs stay in registers as the next layer's A fragments;
 //   * training (k_abc_train) is a per-sample forward and backward pass in
 //     FP32 with the same roundings (straight-through), block sums of the
-//     gradients, and Adam (k_abc_adam) on FP32 master weights.  The loss of
+//     gradients added up in block order (k_abc_reduce: training is
+//     reproducible bit for bit), and Adam (k_abc_adam) on FP32 master
+//     weights.  The loss of
 //     a sample is sum_c (sigmoid(y_c) a_c - b_c)^2 with a = (u_g(t) -
 //     u_i(t+1)) / s and b = (u_g(t+1) - u_i(t)) / s: the update's error
 //     when the neighbour's next value is the true one.
@@ -53,6 +55,7 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "../../include/fletcher_gb300.h"
@@ -311,24 +314,81 @@ __device__ __forceinline__ uint32_t mix32(uint32_t a, uint32_t b) {
 // taken; cells whose stencils are below `min_scale` carry no wave and are
 // skipped.  The next values are the plain update of original/sample.h:32-89
 // (u(t+1) = 2 u(t) - u(t-1) + dt^2 rhs) on the padded field.
-__global__ void k_abc_collect(const float2 *cur, const float2 *prev, const float *coef, const __grid_constant__ Ghost G, int sy, int pitch,
-                              float dx, float dy, float dz, float dt, float keep_frac, uint32_t seed, float min_scale,
-                              float *feat, float *tgt, int4 *pos, unsigned long long *count, unsigned long long cap) {
-  const long n = G.off[6];
-  const Box all = {{0, 0, 0}, {0, 0, 0}};  // empty kept box: the whole field counts
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    if ((mix32(seed, (uint32_t)i) >> 8) * (1.0f / 16777216.0f) >= keep_frac) continue;
-    int c[3], f, a, sgn;
-    const int d = ghost_cell(G, i, c, f, a, sgn);
-    float v[kSt];
-    normal_stencil(cur, c[0], c[1], c[2], a, sgn, G.keep, sy, pitch, v, v + 9);
-    normal_stencil(prev, c[0], c[1], c[2], a, sgn, G.keep, sy, pitch, v + 18, v + 27);
-    float s = 0.f;
+//
+// The samples land in cell order, so the training set does not depend on
+// thread timing: block b takes the cells [b per, (b+1) per); a counting
+// pass gives each block's number of samples, their prefix sums (host) its
+// first slot, and the writing pass ranks each cell inside its block with
+// warp ballots.
+
+// Whether ghost cell i becomes a sample; its stencils and scale.
+__device__ __forceinline__ bool collect_cell(const float2 *cur, const float2 *prev, const Ghost &G, long i, int sy,
+                                             int pitch, float keep_frac, uint32_t seed, float min_scale, float (&v)[kSt],
+                                             float &s, int (&c)[3], int &f, int &a, int &sgn, int &d) {
+  if ((mix32(seed, (uint32_t)i) >> 8) * (1.0f / 16777216.0f) >= keep_frac) return false;
+  d = ghost_cell(G, i, c, f, a, sgn);
+  normal_stencil(cur, c[0], c[1], c[2], a, sgn, G.keep, sy, pitch, v, v + 9);
+  normal_stencil(prev, c[0], c[1], c[2], a, sgn, G.keep, sy, pitch, v + 18, v + 27);
+  s = 0.f;
 #pragma unroll
-    for (int k = 0; k < kSt; ++k) s = fmaxf(s, fabsf(v[k]));
-    if (!(s > min_scale) || !(s > kMinScale)) continue;
-    const unsigned long long slot = atomicAdd(count, 1ull);
-    if (slot >= cap) continue;
+  for (int k = 0; k < kSt; ++k) s = fmaxf(s, fabsf(v[k]));
+  return (s > min_scale) && (s > kMinScale);
+}
+
+constexpr int kCollectBlock = 256;
+
+__global__ void __launch_bounds__(kCollectBlock) k_abc_collect_count(const float2 *cur, const float2 *prev,
+                                                                     const __grid_constant__ Ghost G, int sy,
+                                                                     int pitch, float keep_frac, uint32_t seed,
+                                                                     float min_scale, long per, int *block_count) {
+  __shared__ int cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  const long n = G.off[6];
+  const long lo = blockIdx.x * per, hi = min(n, lo + per);
+  int mine = 0;
+  for (long i = lo + threadIdx.x; i < hi; i += kCollectBlock) {
+    float v[kSt], sc;
+    int c[3], f, a, sgn, d;
+    mine += collect_cell(cur, prev, G, i, sy, pitch, keep_frac, seed, min_scale, v, sc, c, f, a, sgn, d) ? 1 : 0;
+  }
+  atomicAdd(&cnt, mine);  // an integer count: the order does not matter
+  __syncthreads();
+  if (threadIdx.x == 0) block_count[blockIdx.x] = cnt;
+}
+
+__global__ void __launch_bounds__(kCollectBlock) k_abc_collect(const float2 *cur, const float2 *prev,
+                                                               const float *coef, const __grid_constant__ Ghost G,
+                                                               int sy, int pitch, float dx, float dy, float dz,
+                                                               float dt, float keep_frac, uint32_t seed,
+                                                               float min_scale, long per, const long *block_first,
+                                                               float *feat, float *tgt, int4 *pos, long cap) {
+  __shared__ int warp_sum[kCollectBlock / 32];
+  const long n = G.off[6];
+  const long lo = blockIdx.x * per, hi = min(n, lo + per);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const Box all = {{0, 0, 0}, {0, 0, 0}};  // empty kept box: the whole field counts
+  long next = block_first[blockIdx.x];  // slot of this block's next sample
+  for (long c0 = lo; c0 < hi; c0 += kCollectBlock) {
+    const long i = c0 + threadIdx.x;
+    float v[kSt], s = 0.f;
+    int c[3] = {0, 0, 0}, f = 0, a = 0, sgn = 1, d = 0;
+    const bool keep =
+        i < hi && collect_cell(cur, prev, G, i, sy, pitch, keep_frac, seed, min_scale, v, s, c, f, a, sgn, d);
+    // Rank in cell order: lanes before this one in the warp, then warps before it.
+    const unsigned ball = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) warp_sum[warp] = __popc(ball);
+    __syncthreads();
+    int before = __popc(ball & ((1u << lane) - 1u)), total = 0;
+#pragma unroll
+    for (int w = 0; w < kCollectBlock / 32; ++w) {
+      before += w < warp ? warp_sum[w] : 0;
+      total += warp_sum[w];
+    }
+    __syncthreads();
+    const long slot = next + before;
+    next += total;
+    if (!keep || slot >= cap) continue;
     pos[slot] = make_int4(c[0], c[1], c[2], f + 8 * d);
     const float inv = 1.0f / s;
     float *fr = feat + slot * kIn;
@@ -712,14 +772,15 @@ constexpr int sX = 41, sH = 33;
 __device__ __forceinline__ float h16(float v) { return __half2float(__float2half_rn(v)); }
 
 // Forward and backward of B samples (index b of the batch: a random sample,
-// or b itself when seed is 0): loss += sum_c (sigmoid(y_c) a_c - b_c)^2 /
-// (2 B), gradients summed into grad.  Weights are used FP16-rounded, hidden
+// or b itself when seed is 0): each block writes its part of the loss
+// sum_c (sigmoid(y_c) a_c - b_c)^2 / (2 B) and of the gradient to its own
+// slots of lpartial and partial.  Weights are used FP16-rounded, hidden
 // pre-activations and activations are rounded to FP16 (as inference does),
 // the derivatives treat the roundings as the identity.  noise > 0 perturbs the
 // stencil inputs.
 __global__ void __launch_bounds__(kTB) k_abc_train(const float *feat, const float *tgt, long nsamp, int B,
-                                                    uint32_t seed, const float *P, float noise, float *grad,
-                                                    float *loss) {
+                                                    uint32_t seed, const float *P, float noise, float *partial,
+                                                    float *lpartial) {
   extern __shared__ float sm[];
   float *W1 = sm, *b1 = W1 + kHid * kIn, *W2 = b1 + kHid, *b2 = W2 + kHid * kHid, *W3 = b2 + kHid,
         *b3 = W3 + kOut * kHid;
@@ -786,9 +847,17 @@ __global__ void __launch_bounds__(kTB) k_abc_train(const float *feat, const floa
     for (int o = 0; o < kHid; ++o) g = fmaf(W2[o * kHid + k], d2v[o], g);
     d1v[k] = g * (1.0f - a1[k] * a1[k]);
   }
+  // The block's loss and gradient sums go to its own slots (summed over the
+  // blocks in order by k_abc_reduce: the result does not depend on timing).
+  __shared__ float wl[kTB / 32];
   for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
-  if ((tid & 31) == 0) atomicAdd(loss, l / (2.0f * (float)B));
+  if ((tid & 31) == 0) wl[tid >> 5] = l;
   __syncthreads();
+  if (tid == 0) {
+    float bl = 0.f;
+    for (int w = 0; w < kTB / 32; ++w) bl += wl[w];
+    lpartial[blockIdx.x] = bl / (2.0f * (float)B);
+  }
   // Block sums of the per-sample gradient terms.
   for (int e = tid; e < kNP; e += kTB) {
     float s = 0.f;
@@ -811,7 +880,22 @@ __global__ void __launch_bounds__(kTB) k_abc_train(const float *feat, const floa
       const int o = e - oB3;
       for (int q = 0; q < kTB; ++q) s += DY[q * 2 + o];
     }
-    atomicAdd(&grad[e], s);
+    partial[(size_t)blockIdx.x * kNP + e] = s;
+  }
+}
+
+// Sums of the training blocks' partial gradients and losses, in block order.
+__global__ void k_abc_reduce(const float *partial, const float *lpartial, int nblocks, float *grad, float *loss) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < kNP) {
+    float g = 0.f;
+    for (int b = 0; b < nblocks; ++b) g += partial[(size_t)b * kNP + e];
+    grad[e] = g;
+  }
+  if (e == 0) {
+    float l = 0.f;
+    for (int b = 0; b < nblocks; ++b) l += lpartial[b];
+    *loss = l;
   }
 }
 
@@ -857,8 +941,9 @@ struct Trainer {
   long adam_t = 0;
   float *feat = nullptr, *tgt = nullptr;
   int4 *pos = nullptr;  // grid cell, face and distance of every sample
-  unsigned long long *count = nullptr;
+  long nsamp = 0;       // samples held (at most cap)
   long cap = 0;
+  bool reserved = false;
 };
 
 struct ResidentLayer {
@@ -1028,8 +1113,8 @@ extern "C" int FLETCHER_AbcReserve(long capacity) {
   if (T.pos) cudaFree(T.pos);
   T.feat = T.tgt = nullptr;
   T.pos = nullptr;
-  if (!T.count) CKA(cudaMalloc(&T.count, sizeof(unsigned long long)));
-  CKA(cudaMemset(T.count, 0, sizeof(unsigned long long)));
+  T.nsamp = 0;
+  T.reserved = true;
   T.cap = capacity;
   if (capacity) {
     CKA(cudaMalloc(&T.feat, (size_t)capacity * kIn * sizeof(float)));
@@ -1039,18 +1124,13 @@ extern "C" int FLETCHER_AbcReserve(long capacity) {
   return FLETCHER_OK;
 }
 
-extern "C" long FLETCHER_AbcSamples(void) {
-  if (!T.count) return 0;
-  unsigned long long c = 0;
-  if (cudaMemcpy(&c, T.count, sizeof(c), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
-  return (long)(c < (unsigned long long)T.cap ? c : (unsigned long long)T.cap);
-}
+extern "C" long FLETCHER_AbcSamples(void) { return T.nsamp; }
 
 extern "C" int FLETCHER_AbcCollect(const int *interior_lo, const int *interior_hi, int layer, float keep_frac,
                                    unsigned seed, float min_scale) {
   const ResidentView v = resident_view();
   if (!v.init) return err(FLETCHER_ERR_ARGS, "AbcCollect needs an FP32 resident state");
-  if (!T.count || !T.cap) return err(FLETCHER_ERR_ARGS, "AbcCollect: call FLETCHER_AbcReserve first");
+  if (!T.reserved || !T.cap) return err(FLETCHER_ERR_ARGS, "AbcCollect: call FLETCHER_AbcReserve first");
   if (!interior_lo || !interior_hi || layer < kRadius + 1)
     return err(FLETCHER_ERR_ARGS, "AbcCollect: bad box or layer");
   Box in;
@@ -1063,11 +1143,34 @@ extern "C" int FLETCHER_AbcCollect(const int *interior_lo, const int *interior_h
       return err(FLETCHER_ERR_ARGS, "AbcCollect: the box and its layer must lie 4 cells inside the updated region");
   }
   const Ghost G = make_ghost(in, layer);
-  k_abc_collect<<<grid_of(G.off[6], 256), 256, 0, v.stream>>>(v.cur, v.prev, v.coef, G, v.sy, v.pitch, v.dx, v.dy,
-                                                               v.dz, v.dt, keep_frac, seed, min_scale, T.feat, T.tgt,
-                                                               T.pos, T.count, (unsigned long long)T.cap);
+  const long n = G.off[6];
+  const int nb = (int)std::max(1L, std::min(1024L, (n + kCollectBlock - 1) / kCollectBlock));
+  const long per = (n + nb - 1) / nb;
+  std::vector<int> cnt(nb);
+  std::vector<long> first(nb);
+  int *d_cnt = nullptr;
+  long *d_first = nullptr;
+  CKA(cudaMalloc(&d_cnt, nb * sizeof(int)));
+  CKA(cudaMalloc(&d_first, nb * sizeof(long)));
+  k_abc_collect_count<<<nb, kCollectBlock, 0, v.stream>>>(v.cur, v.prev, G, v.sy, v.pitch, keep_frac, seed, min_scale,
+                                                          per, d_cnt);
+  CKA(cudaGetLastError());
+  CKA(cudaMemcpyAsync(cnt.data(), d_cnt, nb * sizeof(int), cudaMemcpyDeviceToHost, v.stream));
+  CKA(cudaStreamSynchronize(v.stream));
+  long total = 0;
+  for (int b = 0; b < nb; ++b) {
+    first[b] = T.nsamp + total;
+    total += cnt[b];
+  }
+  CKA(cudaMemcpyAsync(d_first, first.data(), nb * sizeof(long), cudaMemcpyHostToDevice, v.stream));
+  k_abc_collect<<<nb, kCollectBlock, 0, v.stream>>>(v.cur, v.prev, v.coef, G, v.sy, v.pitch, v.dx, v.dy, v.dz, v.dt,
+                                                    keep_frac, seed, min_scale, per, d_first, T.feat, T.tgt, T.pos,
+                                                    T.cap);
   CKA(cudaGetLastError());
   CKA(cudaStreamSynchronize(v.stream));
+  cudaFree(d_cnt);
+  cudaFree(d_first);
+  T.nsamp = std::min(T.cap, T.nsamp + total);
   return FLETCHER_OK;
 }
 
@@ -1089,16 +1192,17 @@ extern "C" int FLETCHER_AbcTrain(int iters, int batch, float lr, unsigned seed, 
     return err(FLETCHER_ERR_ARGS, "AbcTrain: bad arguments");
   cudaStream_t s = stream_of();
   if (train_attr()) return FLETCHER_GetLastError();
-  float *loss = nullptr;
-  CKA(cudaMalloc(&loss, iters * sizeof(float)));
-  CKA(cudaMemsetAsync(loss, 0, iters * sizeof(float), s));
-  CKA(cudaMemsetAsync(T.grad, 0, kNP * sizeof(float), s));
-  const float b1 = 0.9f, b2 = 0.999f;
   const int blocks = (batch + kTB - 1) / kTB;
+  float *loss = nullptr, *partial = nullptr, *lpartial = nullptr;
+  CKA(cudaMalloc(&loss, iters * sizeof(float)));
+  CKA(cudaMalloc(&partial, (size_t)blocks * kNP * sizeof(float)));
+  CKA(cudaMalloc(&lpartial, blocks * sizeof(float)));
+  const float b1 = 0.9f, b2 = 0.999f;
   for (int it = 0; it < iters; ++it) {
     uint64_t st = (uint64_t)seed * 1000003ull + (uint64_t)it;
     const uint32_t sd = (uint32_t)splitmix(st) | 1u;
-    k_abc_train<<<blocks, kTB, kTrainSmem, s>>>(T.feat, T.tgt, ns, batch, sd, T.P, noise, T.grad, loss + it);
+    k_abc_train<<<blocks, kTB, kTrainSmem, s>>>(T.feat, T.tgt, ns, batch, sd, T.P, noise, partial, lpartial);
+    k_abc_reduce<<<(kNP + 255) / 256, 256, 0, s>>>(partial, lpartial, blocks, T.grad, loss + it);
     ++T.adam_t;
     const float lr_t = lr * 0.5f * (1.0f + cosf(3.14159265f * (float)it / (float)iters));
     k_abc_adam<<<(kNP + 255) / 256, 256, 0, s>>>(T.P, T.grad, T.m, T.v, kNP, lr_t, b1, b2, 1e-8f,
@@ -1109,6 +1213,8 @@ extern "C" int FLETCHER_AbcTrain(int iters, int batch, float lr, unsigned seed, 
   if (loss_out) CKA(cudaMemcpyAsync(loss_out, loss, iters * sizeof(float), cudaMemcpyDeviceToHost, s));
   CKA(cudaStreamSynchronize(s));
   cudaFree(loss);
+  cudaFree(partial);
+  cudaFree(lpartial);
   return FLETCHER_OK;
 }
 
@@ -1116,16 +1222,18 @@ extern "C" int FLETCHER_AbcGradient(const float *feat, const float *tgt, int n, 
   if (!T.weights) return err(FLETCHER_ERR_ARGS, "AbcGradient: no network");
   if (!feat || !tgt || !grad || n < 1) return err(FLETCHER_ERR_ARGS, "AbcGradient: bad arguments");
   if (train_attr()) return FLETCHER_GetLastError();
-  float *df = nullptr, *dt = nullptr, *dl = nullptr, *dg = nullptr;
+  const int blocks = (n + kTB - 1) / kTB;
+  float *df = nullptr, *dt = nullptr, *dl = nullptr, *dg = nullptr, *partial = nullptr, *lpartial = nullptr;
   CKA(cudaMalloc(&df, (size_t)n * kIn * sizeof(float)));
   CKA(cudaMalloc(&dt, (size_t)n * kTgt * sizeof(float)));
   CKA(cudaMalloc(&dl, sizeof(float)));
   CKA(cudaMalloc(&dg, kNP * sizeof(float)));
+  CKA(cudaMalloc(&partial, (size_t)blocks * kNP * sizeof(float)));
+  CKA(cudaMalloc(&lpartial, blocks * sizeof(float)));
   CKA(cudaMemcpy(df, feat, (size_t)n * kIn * sizeof(float), cudaMemcpyHostToDevice));
   CKA(cudaMemcpy(dt, tgt, (size_t)n * kTgt * sizeof(float), cudaMemcpyHostToDevice));
-  CKA(cudaMemset(dl, 0, sizeof(float)));
-  CKA(cudaMemset(dg, 0, kNP * sizeof(float)));
-  k_abc_train<<<(n + kTB - 1) / kTB, kTB, kTrainSmem>>>(df, dt, n, n, 0u, T.P, 0.f, dg, dl);
+  k_abc_train<<<blocks, kTB, kTrainSmem>>>(df, dt, n, n, 0u, T.P, 0.f, partial, lpartial);
+  k_abc_reduce<<<(kNP + 255) / 256, 256>>>(partial, lpartial, blocks, dg, dl);
   CKA(cudaGetLastError());
   CKA(cudaMemcpy(grad, dg, kNP * sizeof(float), cudaMemcpyDeviceToHost));
   if (loss) CKA(cudaMemcpy(loss, dl, sizeof(float), cudaMemcpyDeviceToHost));
@@ -1133,6 +1241,8 @@ extern "C" int FLETCHER_AbcGradient(const float *feat, const float *tgt, int n, 
   cudaFree(dt);
   cudaFree(dl);
   cudaFree(dg);
+  cudaFree(partial);
+  cudaFree(lpartial);
   return FLETCHER_OK;
 }
 
@@ -1234,6 +1344,5 @@ extern "C" void FLETCHER_AbcRelease(void) {
   if (T.feat) cudaFree(T.feat);
   if (T.tgt) cudaFree(T.tgt);
   if (T.pos) cudaFree(T.pos);
-  if (T.count) cudaFree(T.count);
   T = Trainer();
 }

@@ -232,3 +232,19 @@ def test_interval_reuses_the_coefficients():
     assert np.array_equal(out[1][0], out[2][0])
     assert not np.array_equal(out[1][1], out[2][1])
     assert np.max(np.abs(out[1][1] - out[2][1])) < 0.1 * np.max(np.abs(out[1][1]))
+
+
+def test_collection_and_training_are_reproducible():
+    """The training set lands in cell order and the gradient sums are added
+    in block order, so collecting and training twice gives the same samples,
+    losses and weights bit for bit."""
+    runs = []
+    for _ in range(2):
+        learned.collect(models=2, n_virtual=16, times=(40, 60), keep=0.5, capacity=200_000)
+        f, t, c = learned.samples()
+        learned.init(5)
+        loss = learned.train(iters=40, batch=1024, lr=3e-3)
+        runs.append((f, t, c, loss, learned.get_weights()))
+    assert len(runs[0][0]) > 100
+    for a, b in zip(runs[0], runs[1]):
+        assert np.array_equal(a, b)
