@@ -391,7 +391,7 @@ def run_learned_form(args, ws, rank, local, group):
     ns = learned.collect(models=64, n_virtual=48, keep=0.1)
     t1 = time.time()
     learned.init(0)
-    loss = learned.train(iters=args.abc_iters, batch=8192, lr=3e-3)
+    loss = learned.train(iters=args.abc_iters, batch=8192, lr=3e-3, noise=args.abc_noise)
     t2 = time.time()
     n, steps = args.abc_interior, args.abc_steps
     res = learned.compare(n=n, steps=steps, nsnap=5,
@@ -428,6 +428,7 @@ def run_learned_form(args, ws, rank, local, group):
                    "snapshots": res["snapshots"],
                    "training": {"models": 64, "samples": ns, "collect_s": round(t1 - t0, 1),
                                 "train_s": round(t2 - t1, 1), "iters": args.abc_iters, "batch": 8192,
+                                "input_noise": args.abc_noise,
                                 "loss_first": float(loss[:20].mean()), "loss_last": float(loss[-50:].mean())}},
         "speedup_vs_random": round(rv["ms_per_step"] / lv["ms_per_step"], 3),
         "reflected_energy_learned": fin(lv["reflected_energy"]),
@@ -485,6 +486,7 @@ def main():
     ap.add_argument("--abc-interior", type=int, default=256)
     ap.add_argument("--abc-steps", type=int, default=1500)
     ap.add_argument("--abc-iters", type=int, default=3000, help="Adam steps of the learned layer's training")
+    ap.add_argument("--abc-noise", type=float, default=0.0, help="input noise (std) in the learned layer's training")
     ap.add_argument("--no-forms", action="store_true", help="skip timing the other storage forms")
     ap.add_argument("--form-steps", type=int, default=200, help="timed steps of each other storage form")
     ap.add_argument("--shots", type=int, default=48)
