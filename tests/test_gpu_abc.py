@@ -12,8 +12,9 @@ the CPU oracle (oracle/abc_mlp.py).
   the oracle's box-scheme update of the plain step (1e-6), the learned form
   equals it with the oracle network's coefficients (1e-2 of the update's
   size), and nothing outside the ghost zone changes;
-* end to end on a small case: training lowers the loss, the one-way forms
-  stay stable, and the reflected-energy harness measures every form.
+* end to end at 96^3: training lowers the loss, and the learned layer
+  reflects clearly less than the one-way layer without the network and the
+  32-cell random shell.
 """
 import numpy as np
 import pytest
@@ -183,23 +184,29 @@ def test_resident_oneway_steps_vs_cpu_oracle():
 
 
 def test_training_and_reflected_energy_small():
-    """Training on small padded models lowers the loss; the one-way forms
-    stay bounded and reflect less than the bare 8-cell layer; the harness
-    measures every form against the wide-domain run."""
-    n_s = learned.collect(models=12, n_virtual=32, times=range(40, 281, 20), keep=0.3, capacity=2_000_000)
-    assert n_s > 30000
+    """What the trained network gains over the method without it.  Training on
+    32 padded models (the library's kernels, reproducible), then the
+    reflected energy of each form against the wide-domain run at 96^3 x 900
+    steps.  The one-way layer with the medium's coefficients (the method
+    without the network) and the learned one both beat the bare 8-cell
+    layer, and the learned layer reflects clearly less than both the one-way
+    layer and the 32-cell random shell (measured 0.0071 vs 0.0112 and
+    0.0102)."""
+    n_s = learned.collect(models=32, n_virtual=48, keep=0.1, capacity=3_000_000)
+    assert n_s > 500_000
     learned.init(0)
-    loss = learned.train(iters=800, batch=4096, lr=3e-3)
+    loss = learned.train(iters=3000, batch=8192, lr=3e-3)
     print(f"samples {n_s}, loss {loss[:20].mean():.4g} -> {loss[-50:].mean():.4g}")
-    assert loss[-50:].mean() < 0.7 * loss[:20].mean()
-    res = learned.compare(n=48, steps=600, nsnap=3)
+    assert loss[-50:].mean() < 0.3 * loss[:20].mean()
+    res = learned.compare(n=96, steps=900, nsnap=3, kinds=("random", "learned", "oneway", "plain8"))
     for k, v in res.items():
         print(k, v)
-    assert res["wide"]["reflected_energy"] == 0.0
-    plain = res["plain8"]["reflected_energy"]
-    assert 0.0 < res["random"]["reflected_energy"] < plain
-    assert 0.0 < res["oneway"]["reflected_energy"] < plain
-    assert 0.0 < res["learned"]["reflected_energy"] < plain
+    e = {k: v["reflected_energy"] for k, v in res.items() if k != "snapshots"}
+    assert e["wide"] == 0.0
+    assert 0.0 < e["random"] < e["plain8"]
+    assert 0.0 < e["oneway"] < e["plain8"]
+    assert 0.0 < e["learned"] < 0.8 * e["oneway"]
+    assert e["learned"] < e["random"]
     assert res["learned"]["launches_per_step"] == 5 and res["oneway"]["launches_per_step"] == 4
 
 
