@@ -327,8 +327,9 @@ def run_batch_form(args, ws, rank, local, group):
 
     torch.cuda.set_device(local)
     spec = multishot_spec(args.shots, seed=args.seed + rank)
+    form = args.batch_form
     t0 = time.time()
-    batch = Batch()
+    batch = Batch(form=form)
     for p in spec:
         batch.add(p)
     setup_s = time.time() - t0
@@ -345,7 +346,7 @@ def run_batch_form(args, ws, rank, local, group):
     if not args.no_sequential:
         stream = torch.cuda.Stream()
         for p in spec:
-            prop = Propagator(stream=stream.cuda_stream)
+            prop = Propagator(stream=stream.cuda_stream, form=form)
             prop.initialize(p.sx, p.sy, p.sz, p.bord, p.dx, p.dy, p.dz, p.dt, p.model())
             ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             ev0.record(stream)
@@ -359,9 +360,11 @@ def run_batch_form(args, ws, rank, local, group):
     line = {
         "metric": "MSamples/s, batched shots (C3)", "value": round(value, 1), "unit": UNIT, "n_gpus": ws,
         "steps": max(p.steps for p in spec), "ms_total": round(ms_max, 1), "higher_is_better": True,
-        "scaling": "weak", "dtype": "f32", "data": "synthetic (48 seeded layered TTI shots)",
+        "scaling": "weak", "dtype": "f32" if form == "fp32" else f"f32 arithmetic, {form} storage",
+        "data": "synthetic (48 seeded layered TTI shots)",
         "config": {"workload": f"C3: {len(spec)} shots, n ~ U{{96..320}}/8*8 per axis, 500-1500 steps, dt 0.6 ms, "
                                "one persistent launch per step, CUDA-graph time loop",
+                   "storage": form,
                    "cell_steps": info["cell_steps"], "device_gb": round(info["device_bytes"] / 1e9, 1),
                    "setup_s": round(setup_s, 1), "tile": tune["tile"], "autotune": tune["ms_per_step"]},
         "gpu_launches": info["launches"],
@@ -490,6 +493,8 @@ def main():
     ap.add_argument("--no-forms", action="store_true", help="skip timing the other storage forms")
     ap.add_argument("--form-steps", type=int, default=200, help="timed steps of each other storage form")
     ap.add_argument("--shots", type=int, default=48)
+    ap.add_argument("--batch-form", default="fp32", choices=["fp32", "fp16", "fp16x"],
+                    help="storage form of the batched shots (--form batch)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-sequential", action="store_true")
     args = ap.parse_args()

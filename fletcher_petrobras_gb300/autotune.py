@@ -12,6 +12,7 @@ import json
 import os
 
 CANDIDATES = [(16, 5), (16, 4), (12, 5), (12, 4), (12, 6), (8, 5)]
+HALF_CANDIDATES = [(16, 5), (16, 4), (12, 5), (12, 4), (12, 6), (8, 6)]  # built 16-bit shapes
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 
 
@@ -40,12 +41,15 @@ def _store(path, data):
     os.replace(tmp, path)
 
 
-def tune_batch(batch, steps: int = 20, cache: str | None = DEFAULT_CACHE, candidates=CANDIDATES) -> dict:
+def tune_batch(batch, steps: int = 20, cache: str | None = DEFAULT_CACHE, candidates=None) -> dict:
     """Chooses the batch's tile shape: cached, or timed over `steps` steps per
     candidate (the fields are zeroed afterwards).  Returns the record."""
     from .batch import shape_class
 
-    key = f"{gpu_name()}|fp32|{shape_class(batch.probs)}"
+    form = getattr(batch, "form", "fp32")
+    if candidates is None:
+        candidates = CANDIDATES if form == "fp32" else HALF_CANDIDATES
+    key = f"{gpu_name()}|{form}|{shape_class(batch.probs)}"
     data = _load(cache) if cache else {}
     if key in data:
         rec = data[key]

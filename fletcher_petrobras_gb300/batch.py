@@ -15,7 +15,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import fptr
-from .driver import FletcherError, _check
+from .driver import FORMS, FletcherError, _check
 from .models import Problem
 
 
@@ -38,9 +38,15 @@ def multishot_spec(nshots: int = 48, seed: int = 0, nmin: int = 96, nmax: int = 
 class Batch:
     """A batch of shots resident on the GPU (one per process)."""
 
-    def __init__(self, bord=4, dx=12.5, dy=12.5, dz=12.5, dt=0.0006):
+    def __init__(self, bord=4, dx=12.5, dy=12.5, dz=12.5, dt=0.0006, form: str = "fp32"):
+        """form: storage form of every shot's fields ("fp32", "fp16", "fp16x")."""
         self.lib = _lib.load()
         self.lib.FLETCHER_ClearError()
+        if form not in FORMS:
+            raise ValueError(f"unknown form {form!r}; one of {sorted(FORMS)}")
+        self.form = form
+        if self.lib.FLETCHER_SetForm(FORMS[form]):
+            _check(self.lib, "SetForm")
         if self.lib.FLETCHER_BatchCreate(bord, dx, dy, dz, dt):
             _check(self.lib, "FLETCHER_BatchCreate")
         self.dt = dt

@@ -1144,13 +1144,20 @@ struct BatchShot {
   int sx = 0, sy = 0, sz = 0, pitch = 0, nsteps = 0;
   long isrc = 0;
   size_t n = 0, npitch = 0;
-  float2 *F[2] = {nullptr, nullptr};
+  float2 *F[2] = {nullptr, nullptr};  // FP32 form
+  // 16-bit forms: the two field buffers (half2 per cell, residual bytes),
+  // per-plane exponents [3][sz] and maxima [2][sz].
+  unsigned *Hh[2] = {nullptr, nullptr};
+  unsigned short *Hl[2] = {nullptr, nullptr};
+  int *E = nullptr;
+  unsigned *Mx = nullptr;
   float *coef = nullptr;
   int ntx = 0, nty = 0, chunk = 0, nchunk = 0;
 };
 
 struct Batch {
   bool open = false;
+  int form = FLETCHER_FORM_FP32;  // storage form of every shot (fixed at creation)
   int bord = 4;
   float dx = 0, dy = 0, dz = 0, dt = 0;
   std::vector<BatchShot> shots;
@@ -1160,6 +1167,9 @@ struct Batch {
   ShotDesc *d_desc = nullptr;
   ShotMaps *d_maps = nullptr;
   int4 *d_items = nullptr;
+  HalfShot *d_hshots = nullptr;     // 16-bit forms
+  HalfShotMaps *d_hmaps = nullptr;
+  int *d_order = nullptr;
   float *scratch = nullptr;
   size_t max_n = 0;
   int rows = 12, stages = 5;
@@ -1175,17 +1185,28 @@ void batch_free_tables() {
   if (B.d_desc) cudaFree(B.d_desc);
   if (B.d_maps) cudaFree(B.d_maps);
   if (B.d_items) cudaFree(B.d_items);
+  if (B.d_hshots) cudaFree(B.d_hshots);
+  if (B.d_hmaps) cudaFree(B.d_hmaps);
+  if (B.d_order) cudaFree(B.d_order);
   B.d_desc = nullptr;
   B.d_maps = nullptr;
   B.d_items = nullptr;
+  B.d_hshots = nullptr;
+  B.d_hmaps = nullptr;
+  B.d_order = nullptr;
   B.sealed_rows = 0;
 }
 
 void batch_free() {
   batch_free_tables();
   for (auto &s : B.shots) {
-    if (s.F[0]) cudaFree(s.F[0]);
-    if (s.F[1]) cudaFree(s.F[1]);
+    for (int b = 0; b < 2; ++b) {
+      if (s.F[b]) cudaFree(s.F[b]);
+      if (s.Hh[b]) cudaFree(s.Hh[b]);
+      if (s.Hl[b]) cudaFree(s.Hl[b]);
+    }
+    if (s.E) cudaFree(s.E);
+    if (s.Mx) cudaFree(s.Mx);
     if (s.coef) cudaFree(s.coef);
   }
   if (B.scratch) cudaFree(B.scratch);
@@ -1194,9 +1215,15 @@ void batch_free() {
 }
 
 // Work list, descriptors and TMA descriptors for tile height `rows`.
+bool batch_half() { return B.form != FLETCHER_FORM_FP32; }
+
+bool batch_shape_built(int rows, int stages) {
+  return batch_half() ? propagate_half_supported(rows, stages) : propagate_fp32_supported(rows, stages);
+}
+
 int batch_seal(int rows, int stages) {
-  if (!propagate_fp32_supported(rows, stages))
-    return fail(FLETCHER_ERR_ARGS, "tile shape (%d rows, %d stages) is not built", rows, stages);
+  if (!batch_shape_built(rows, stages))
+    return fail(FLETCHER_ERR_ARGS, "tile shape (%d rows, %d stages) is not built for form %d", rows, stages, B.form);
   if (B.sealed_rows == rows) {
     B.stages = stages;
     return FLETCHER_OK;
@@ -1205,6 +1232,8 @@ int batch_seal(int rows, int stages) {
   const int ns = (int)B.shots.size();
   std::vector<ShotDesc> desc(ns);
   std::vector<ShotMaps> maps(ns);
+  std::vector<HalfShot> hshots(ns);
+  std::vector<HalfShotMaps> hmaps(ns);
   std::vector<int4> items;
   B.order.resize(ns);
   for (int i = 0; i < ns; ++i) B.order[i] = i;
@@ -1221,6 +1250,16 @@ int batch_seal(int rows, int stages) {
     s.chunk = (depth + s.nchunk - 1) / s.nchunk;
     s.nchunk = (depth + s.chunk - 1) / s.chunk;
     if (build_maps(&maps[i], s.F, s.coef, s.sx, s.sy, s.sz, s.pitch, rows)) return g_last_err;
+    if (batch_half()) {
+      if (build_half_maps(hmaps[i].m, s.Hh, s.Hl, maps[i], s.sx, s.sy, s.sz, s.pitch, rows)) return g_last_err;
+      HalfShot &h = hshots[i];
+      for (int b = 0; b < 2; ++b) {
+        h.hi[b] = s.Hh[b];
+        h.lo[b] = s.Hl[b];
+      }
+      h.E = s.E;
+      h.Mx = s.Mx;
+    }
     ShotDesc &d = desc[i];
     memset(&d, 0, sizeof(d));
     d.F[0] = s.F[0];
@@ -1242,6 +1281,14 @@ int batch_seal(int rows, int stages) {
   CK(cudaMemcpy(B.d_desc, desc.data(), sizeof(ShotDesc) * ns, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(B.d_maps, maps.data(), sizeof(ShotMaps) * ns, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(B.d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
+  if (batch_half()) {
+    CK(cudaMalloc(&B.d_hshots, sizeof(HalfShot) * ns));
+    CK(cudaMalloc(&B.d_hmaps, sizeof(HalfShotMaps) * ns));
+    CK(cudaMalloc(&B.d_order, sizeof(int) * ns));
+    CK(cudaMemcpy(B.d_hshots, hshots.data(), sizeof(HalfShot) * ns, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(B.d_hmaps, hmaps.data(), sizeof(HalfShotMaps) * ns, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(B.d_order, B.order.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
+  }
   B.sealed_rows = rows;
   B.stages = stages;
   return FLETCHER_OK;
@@ -1284,6 +1331,26 @@ int batch_issue(int it0, int it1, const float *src) {
     P.src = src[it];
     P.cor = it > 0 ? src[it - 1] : 0.0f;
     L.grid = P.nitems < ctas ? P.nitems : ctas;
+    if (batch_half()) {
+      // The new field's plane exponents (every running shot, one launch),
+      // then the step; the current field uses exponent slot it % 3.
+      const int ecur = it % 3;
+      CK(half_scales_batch(B.d_hshots, B.d_desc, B.d_order, active, P.parity, ecur, fabsf(P.src) + fabsf(P.cor),
+                           g_stream));
+      HalfLaunch HL;
+      memset(&HL, 0, sizeof(HL));
+      HL.h.p = P;
+      HL.h.hshots = B.d_hshots;
+      HL.h.hmaps = B.d_hmaps;
+      HL.h.ecur = ecur;
+      HL.tile_rows = L.tile_rows;
+      HL.stages = L.stages;
+      HL.grid = L.grid;
+      HL.batch = true;
+      CK(propagate_half_launch(HL, B.form == FLETCHER_FORM_FP16X, g_stream));
+      B.launches += 2;
+      continue;
+    }
     CK(propagate_fp32_launch(L, g_stream));
     ++B.launches;
   }
@@ -1306,8 +1373,9 @@ extern "C" int FLETCHER_BatchCreate(int bord, float dx, float dy, float dz, floa
   B.open = true;
   B.bord = bord;
   B.dx = dx; B.dy = dy; B.dz = dz; B.dt = dt;
+  B.form = g_form;
   B.rows = g_req_rows ? g_req_rows : 16;
-  B.stages = g_req_stages ? g_req_stages : 5;
+  B.stages = g_req_stages ? g_req_stages : (B.form == FLETCHER_FORM_FP16 ? 4 : 5);
   return FLETCHER_OK;
 }
 
@@ -1326,18 +1394,39 @@ extern "C" int FLETCHER_BatchAddShot(int sx, int sy, int sz, const float *model,
       z >= sz - b)
     return -fail(FLETCHER_ERR_ARGS, "batched source %ld must lie in the updated region", iSource);
   cudaStream_t st = g_stream;
-  if (cudaMalloc(&s.F[0], s.npitch * sizeof(float2)) != cudaSuccess ||
-      cudaMalloc(&s.F[1], s.npitch * sizeof(float2)) != cudaSuccess ||
-      cudaMalloc(&s.coef, s.npitch * kNumCoef * sizeof(float)) != cudaSuccess) {
-    if (s.F[0]) cudaFree(s.F[0]);
-    if (s.F[1]) cudaFree(s.F[1]);
-    if (s.coef) cudaFree(s.coef);
-    cudaGetLastError();
-    return -fail(FLETCHER_ERR_NOMEM, "device allocation for shot %zu failed", B.shots.size());
+  const bool half = batch_half(), ext = B.form == FLETCHER_FORM_FP16X;
+  // Field buffers of the shot's form (zeroed below), the coefficients and a
+  // temporary for the raw model; everything is released on failure.
+  const size_t fbytes = half ? s.npitch * sizeof(unsigned) : s.npitch * sizeof(float2);
+  bool ok = true;
+  for (int b = 0; b < 2; ++b) {
+    if (half) {
+      ok = ok && cudaMalloc(&s.Hh[b], fbytes) == cudaSuccess;
+      if (ext) ok = ok && cudaMalloc(&s.Hl[b], s.npitch * sizeof(unsigned short)) == cudaSuccess;
+    } else {
+      ok = ok && cudaMalloc(&s.F[b], fbytes) == cudaSuccess;
+    }
   }
+  if (half) {
+    ok = ok && cudaMalloc(&s.E, 3 * sz * sizeof(int)) == cudaSuccess;
+    ok = ok && cudaMalloc(&s.Mx, 2 * sz * sizeof(unsigned)) == cudaSuccess;
+  }
+  ok = ok && cudaMalloc(&s.coef, s.npitch * kNumCoef * sizeof(float)) == cudaSuccess;
   float *raw = nullptr;
-  if (cudaMalloc(&raw, 6 * s.n * sizeof(float)) != cudaSuccess) {
-    cudaFree(s.F[0]); cudaFree(s.F[1]); cudaFree(s.coef);
+  ok = ok && cudaMalloc(&raw, 6 * s.n * sizeof(float)) == cudaSuccess;
+  auto release = [&]() {
+    for (int b = 0; b < 2; ++b) {
+      if (s.F[b]) cudaFree(s.F[b]);
+      if (s.Hh[b]) cudaFree(s.Hh[b]);
+      if (s.Hl[b]) cudaFree(s.Hl[b]);
+    }
+    if (s.E) cudaFree(s.E);
+    if (s.Mx) cudaFree(s.Mx);
+    if (s.coef) cudaFree(s.coef);
+    if (raw) cudaFree(raw);
+  };
+  if (!ok) {
+    release();
     cudaGetLastError();
     return -fail(FLETCHER_ERR_NOMEM, "device allocation for shot %zu failed", B.shots.size());
   }
@@ -1349,12 +1438,21 @@ extern "C" int FLETCHER_BatchAddShot(int sx, int sy, int sz, const float *model,
     k_precompute<<<grid_for(s.n), 256, 0, st>>>(r6, s.coef, sx, sy, sz, s.pitch);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = cudaMemsetAsync(s.F[0], 0, s.npitch * sizeof(float2), st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(s.F[1], 0, s.npitch * sizeof(float2), st);
+  for (int b = 0; b < 2; ++b) {
+    if (e == cudaSuccess) e = cudaMemsetAsync(half ? (void *)s.Hh[b] : (void *)s.F[b], 0, fbytes, st);
+    if (e == cudaSuccess && s.Hl[b]) e = cudaMemsetAsync(s.Hl[b], 0, s.npitch * sizeof(unsigned short), st);
+  }
+  if (e == cudaSuccess && half) e = cudaMemsetAsync(s.E, 0, 3 * sz * sizeof(int), st);
+  if (e == cudaSuccess && half) e = cudaMemsetAsync(s.Mx, 0, 2 * sz * sizeof(unsigned), st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   cudaFree(raw);
-  if (e != cudaSuccess) return -fail(FLETCHER_ERR_CUDA, "shot set-up: %s", cudaGetErrorString(e));
-  B.dev_bytes += 2 * s.npitch * sizeof(float2) + s.npitch * kNumCoef * sizeof(float);
+  raw = nullptr;
+  if (e != cudaSuccess) {
+    release();
+    return -fail(FLETCHER_ERR_CUDA, "shot set-up: %s", cudaGetErrorString(e));
+  }
+  B.dev_bytes += 2 * fbytes + s.npitch * kNumCoef * sizeof(float);
+  if (half) B.dev_bytes += (ext ? 2 * s.npitch * sizeof(unsigned short) : 0) + 5 * sz * sizeof(int);
   if (s.n > B.max_n) {
     if (B.scratch) cudaFree(B.scratch);
     B.scratch = nullptr;
@@ -1372,8 +1470,13 @@ extern "C" int FLETCHER_BatchAddShot(int sx, int sy, int sz, const float *model,
 extern "C" int FLETCHER_BatchReset(void) {
   if (!B.open) return fail(FLETCHER_ERR_ARGS, "no batch");
   for (auto &s : B.shots) {
-    CK(cudaMemsetAsync(s.F[0], 0, s.npitch * sizeof(float2), g_stream));
-    CK(cudaMemsetAsync(s.F[1], 0, s.npitch * sizeof(float2), g_stream));
+    for (int b = 0; b < 2; ++b) {
+      if (s.F[b]) CK(cudaMemsetAsync(s.F[b], 0, s.npitch * sizeof(float2), g_stream));
+      if (s.Hh[b]) CK(cudaMemsetAsync(s.Hh[b], 0, s.npitch * sizeof(unsigned), g_stream));
+      if (s.Hl[b]) CK(cudaMemsetAsync(s.Hl[b], 0, s.npitch * sizeof(unsigned short), g_stream));
+    }
+    if (s.E) CK(cudaMemsetAsync(s.E, 0, 3 * s.sz * sizeof(int), g_stream));
+    if (s.Mx) CK(cudaMemsetAsync(s.Mx, 0, 2 * s.sz * sizeof(unsigned), g_stream));
   }
   CK(cudaStreamSynchronize(g_stream));
   return FLETCHER_OK;
@@ -1387,8 +1490,10 @@ extern "C" int FLETCHER_BatchRun(const float *src, int max_steps, int use_graph,
   if (max_steps > 0 && max_steps < steps) steps = max_steps;
   B.src.assign(src, src + steps);
   // Kernel attributes are set outside any capture.
-  if (propagate_fp32_prepare(B.sealed_rows, B.stages) != cudaSuccess)
-    return fail(FLETCHER_ERR_CUDA, "kernel attribute set-up failed");
+  const cudaError_t pe = batch_half()
+                            ? propagate_half_prepare(B.sealed_rows, B.stages, B.form == FLETCHER_FORM_FP16X, true)
+                            : propagate_fp32_prepare(B.sealed_rows, B.stages);
+  if (pe != cudaSuccess) return fail(FLETCHER_ERR_CUDA, "kernel attribute set-up failed");
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -1428,10 +1533,17 @@ extern "C" int FLETCHER_BatchGetField(int shot, int which, float *host) {
   if (!B.open || shot < 0 || shot >= (int)B.shots.size() || which < 0 || which > 3 || !host)
     return fail(FLETCHER_ERR_ARGS, "bad shot %d or field %d", shot, which);
   const BatchShot &s = B.shots[shot];
-  // After nsteps steps the current field is in F[nsteps & 1].
+  // After nsteps steps the current field is in buffer nsteps & 1 (16-bit
+  // forms: with exponent slot nsteps % 3, the previous field's two slots on).
   const int buf = which < 2 ? (s.nsteps & 1) : ((s.nsteps + 1) & 1);
-  k_unpack<<<grid_for(s.n), 256, 0, g_stream>>>(s.F[buf], B.scratch, which & 1, s.sx, s.sy, s.sz, s.pitch);
-  CK(cudaGetLastError());
+  if (batch_half()) {
+    const int slot = which < 2 ? s.nsteps % 3 : (s.nsteps + 2) % 3;
+    CK(half_decode(s.Hh[buf], s.Hl[buf], s.E + slot * s.sz, B.scratch, which & 1, s.sx, s.sy, s.sz, s.pitch,
+                   B.form == FLETCHER_FORM_FP16X, grid_for(s.n), g_stream));
+  } else {
+    k_unpack<<<grid_for(s.n), 256, 0, g_stream>>>(s.F[buf], B.scratch, which & 1, s.sx, s.sy, s.sz, s.pitch);
+    CK(cudaGetLastError());
+  }
   CK(cudaMemcpyAsync(host, B.scratch, s.n * sizeof(float), cudaMemcpyDeviceToHost, g_stream));
   CK(cudaStreamSynchronize(g_stream));
   // The previous-field buffer lacks the last step's source at the source
@@ -1444,8 +1556,9 @@ extern "C" int FLETCHER_BatchGetField(int shot, int which, float *host) {
 
 extern "C" int FLETCHER_BatchSetTileConfig(int rows, int stages) {
   if (!B.open) return fail(FLETCHER_ERR_ARGS, "no batch");
-  const int r = rows ? rows : 16, s = stages ? stages : 5;
-  if (!propagate_fp32_supported(r, s)) return fail(FLETCHER_ERR_ARGS, "tile shape (%d, %d) is not built", r, s);
+  const int r = rows ? rows : 16, s = stages ? stages : (B.form == FLETCHER_FORM_FP16 ? 4 : 5);
+  if (!batch_shape_built(r, s))
+    return fail(FLETCHER_ERR_ARGS, "tile shape (%d, %d) is not built for form %d", r, s, B.form);
   B.rows = r;
   B.stages = s;
   return FLETCHER_OK;

@@ -96,24 +96,50 @@ struct HalfMaps {
   CUtensorMap arr, upd;          // coefficients, as in the FP32 form
 };
 
+// One batched shot of a 16-bit form (device memory).
+struct HalfShot {
+  unsigned *hi[2];        // the two field buffers: (p, q) as half2 per cell
+  unsigned short *lo[2];  // their residual bytes (extended form; null otherwise)
+  int *E;                 // [3][sz] per-plane exponents; the field of step it uses slot it % 3
+  unsigned *Mx;           // [2][sz] per-plane max |value| (float bits) of the field in buffer b
+};
+
+// A batched shot's tensor maps, by the buffer that holds the current field.
+struct alignas(64) HalfShotMaps {
+  HalfMaps m[2];
+};
+
 struct HalfParams {
   PropParams p;                       // geometry (p.one), spacing, source, error word
   unsigned *out_hi;                   // new field: half2 per cell
   unsigned short *out_lo;             // new field: residual bytes (extended form)
   const int *e_cur, *e_prev, *e_new;  // per-plane exponents of the current, previous and new field
   unsigned *m_new;                    // per-plane max |value| of the new field (float bits), atomicMax
+  // Batched launches (p.items, p.shots): per-shot buffers and maps, and the
+  // exponent slot of the current field (step % 3).
+  const HalfShot *hshots;
+  const HalfShotMaps *hmaps;
+  int ecur;
 };
 
 struct HalfLaunch {
   HalfParams h;
   HalfMaps m;
   int tile_rows, stages, grid;
+  bool batch;  // h.p.items / h.p.shots / h.hshots / h.hmaps describe the work
 };
 
 bool propagate_half_supported(int tile_rows, int stages);
 cudaError_t propagate_half_launch(const HalfLaunch &L, bool ext, cudaStream_t s);
+cudaError_t propagate_half_prepare(int tile_rows, int stages, bool ext, bool batch);
 cudaError_t half_scales(const unsigned *m_cur, unsigned *m_prev, int *e_new, int sz, int src_z, float src_abs,
                         cudaStream_t s);
+// Before a batched 16-bit step: the new field's plane exponents and the
+// cleared maxima (as half_scales) of the first `active` shots of `order`,
+// block i taking shot order[i]; the current field is in buffer c, its
+// exponents in slot ecur.
+cudaError_t half_scales_batch(const HalfShot *hs, const ShotDesc *sd, const int *order, int active, int c, int ecur,
+                              float src_abs, cudaStream_t s);
 cudaError_t half_encode(const float *p, const float *q, unsigned *hv, unsigned short *rv, int *e, unsigned *m, int sx,
                         int sy, int sz, int pitch, bool ext, cudaStream_t s);
 cudaError_t half_decode(const unsigned *hv, const unsigned short *rv, const int *e, float *out, int comp, int sx,

@@ -114,16 +114,30 @@ __device__ __forceinline__ void encode(f2 v, float sc, unsigned &hv, unsigned sh
 
 struct HItem {
   int x0, y0, z0, z1;
+  int shot;
 };
 
-// Segment `item` of the launch's list: {x0, y0, z0, z1}.
+// Item `item` of the launch: a segment {x0, y0, z0, z1} of the single shot's
+// list, or (batched) a work item {shot, x0, y0, chunk index}.
+template <bool BATCH>
 __device__ __forceinline__ HItem decode_hitem(int item, const PropParams &P) {
-  const int4 w = P.seg[item];
   HItem it;
-  it.x0 = w.x;
-  it.y0 = w.y;
-  it.z0 = w.z;
-  it.z1 = w.w;
+  if constexpr (BATCH) {
+    const int4 w = P.items[item];
+    const ShotDesc &d = P.shots[w.x];
+    it.x0 = w.y;
+    it.y0 = w.z;
+    it.z0 = d.bord + w.w * d.chunk;
+    it.z1 = min(it.z0 + d.chunk, d.sz - d.bord);
+    it.shot = w.x;
+  } else {
+    const int4 w = P.seg[item];
+    it.x0 = w.x;
+    it.y0 = w.y;
+    it.z0 = w.z;
+    it.z1 = w.w;
+    it.shot = 0;
+  }
   return it;
 }
 
@@ -150,12 +164,11 @@ __device__ __forceinline__ void issue_half(unsigned char *stage, uint64_t *bar, 
   }
 }
 
-template <int TY, int S, bool ISO, bool EXT>
+template <int TY, int S, bool ISO, bool EXT, bool BATCH>
 __global__ void __launch_bounds__(kTileX *TY, 1)
     k_propagate_half(const __grid_constant__ HalfMaps M, const __grid_constant__ HalfParams H) {
   using G = GeoH<TY, EXT>;
   const PropParams &P = H.p;
-  const ShotDesc &sd = P.one;
   constexpr int NTH = kTileX * TY;
   extern __shared__ unsigned char smem_dyn[];
   unsigned char *smem = smem_dyn + ((128u - (smem_addr(smem_dyn) & 127u)) & 127u);
@@ -170,24 +183,32 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
   volatile int *s_end = ctl + 3;                           // end of this CTA's segments
   unsigned *smax = reinterpret_cast<unsigned *>(ctl + 4);  // CTA max of the plane updated, by step parity
   volatile int *s_pend = ctl + 6;  // plane whose CTA maximum waits in smax[sel ^ 1] (-1: none)
+  volatile int *s_pend_shot = ctl + 7;  // and its shot (batched launches)
 
   const int tid = threadIdx.x;
   const int lx = tid & 31;
   const int ly = tid >> 5;
-  // This CTA's segments: cta_first[b] .. cta_first[b + 1] - 1.  The end
-  // and thread 0's pending plane live in shared memory (no loop registers).
-  const int item_first = P.cta_first[blockIdx.x];
-  if (item_first >= P.cta_first[blockIdx.x + 1]) return;
-  auto item_end = [&]() { return *s_end; };
+  // This CTA's items: its segments cta_first[b] .. cta_first[b + 1] - 1,
+  // or (batched) items b, b + grid, ... below nitems.  The end and thread
+  // 0's pending plane live in shared memory (no loop registers).
+  const int item_first = BATCH ? (int)blockIdx.x : P.cta_first[blockIdx.x];
+  if (item_first >= (BATCH ? P.nitems : P.cta_first[blockIdx.x + 1])) return;
+  auto item_end = [&]() { return BATCH ? P.nitems : *s_end; };
+  auto item_step = [&]() { return BATCH ? (int)gridDim.x : 1; };
+  // Tensor maps of an item: the shot's (batched) or the launch's.
+  auto maps_of = [&](const HItem &it) -> const HalfMaps & {
+    if constexpr (BATCH) return H.hmaps[it.shot].m[P.parity];
+    else return M;
+  };
   const bool producer = tid == (TY - 1) * 32;
   auto produce = [&]() {
     int item = cur[0], k = cur[1], stg = cur[2];
-    const HItem it = decode_hitem(item, P);
-    issue_half<TY, EXT>(smem + stg * G::STAGE_B, &full[stg], it, k, M);
+    const HItem it = decode_hitem<BATCH>(item, P);
+    issue_half<TY, EXT>(smem + stg * G::STAGE_B, &full[stg], it, k, maps_of(it));
     if (++stg == S) stg = 0;
     if (++k >= it.z1 + kRadius) {
-      ++item;
-      if (item < item_end()) k = decode_hitem(item, P).z0 - kRadius;
+      item += item_step();
+      if (item < item_end()) k = decode_hitem<BATCH>(item, P).z0 - kRadius;
     }
     cur[0] = item;
     cur[1] = k;
@@ -198,22 +219,39 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
     mbar_init(xchg, TY);
     mbar_fence_init();
     cur[0] = item_first;
-    cur[1] = decode_hitem(item_first, P).z0 - kRadius;
+    cur[1] = decode_hitem<BATCH>(item_first, P).z0 - kRadius;
     cur[2] = 0;
-    *s_end = P.cta_first[blockIdx.x + 1];
+    if constexpr (!BATCH) *s_end = P.cta_first[blockIdx.x + 1];
     *s_pend = -1;
+    *s_pend_shot = 0;
     smax[0] = smax[1] = 0u;
   }
   __syncthreads();
   if (producer) {
-    tma_prefetch_desc(&M.cur_hi);
-    tma_prefetch_desc(&M.prev_hi);
-    tma_prefetch_desc(&M.arr);
-    tma_prefetch_desc(&M.upd);
+    if constexpr (!BATCH) {
+      tma_prefetch_desc(&M.cur_hi);
+      tma_prefetch_desc(&M.prev_hi);
+      tma_prefetch_desc(&M.arr);
+      tma_prefetch_desc(&M.upd);
+    }
     // Prologue: S-1 steps; afterwards each step refills the stage freed by
     // the step before it.
     for (int a = 0; a < S - 1 && cur[0] < item_end(); ++a) produce();
   }
+  // Exponents and maxima of the new field of a shot (batched: the shot's
+  // buffers, where the current field is in buffer parity and exponent slot
+  // ecur; otherwise the launch's own arrays).
+  auto e_slot = [&](int shot, int d) -> const int * {
+    return H.hshots[shot].E + ((H.ecur + d) % 3) * P.shots[shot].sz;
+  };
+  auto e_new_of = [&](int shot) -> const int * {
+    if constexpr (BATCH) return e_slot(shot, 1);
+    else return H.e_new;
+  };
+  auto m_new_of = [&](int shot) -> unsigned * {
+    if constexpr (BATCH) return H.hshots[shot].Mx + (1 - P.parity) * P.shots[shot].sz;
+    else return H.m_new;
+  };
 
   const float sx1 = P.inv_dx, sy1 = P.inv_dy, sz1 = P.inv_dz;
   const float sxx = P.inv_dxx, syy = P.inv_dyy, szz = P.inv_dzz;
@@ -221,15 +259,26 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
   const int hr = ly * 4 + (lx >> 3);
   const int hxc = (lx & 7) < 4 ? (lx & 7) : G::TX + (lx & 7);
   const int hh = (hr + kRadius) * G::HX + hxc;
-  const long plane = (long)sd.pitch * sd.sy;
 
   int stage = 0;
   uint32_t phase = 0, xphase = 0;
   int sel = 0;
   int abw = 0;  // shared A/B ring slot of the arriving plane (the plane 4 back is at abw + 1)
   bool bad = false;
-  for (int item = item_first; item < item_end(); ++item) {
-    const HItem it = decode_hitem(item, P);
+  for (int item = item_first; item < item_end(); item += item_step()) {
+    const HItem it = decode_hitem<BATCH>(item, P);
+    const ShotDesc &sd = BATCH ? P.shots[it.shot] : P.one;
+    const long plane = (long)sd.pitch * sd.sy;
+    const int *e_cur = H.e_cur, *e_prev = H.e_prev, *e_new = H.e_new;
+    unsigned *out_hi = H.out_hi;
+    unsigned short *out_lo = H.out_lo;
+    if constexpr (BATCH) {
+      e_cur = e_slot(it.shot, 0);
+      e_new = e_slot(it.shot, 1);
+      e_prev = e_slot(it.shot, 2);
+      out_hi = H.hshots[it.shot].hi[1 - P.parity];
+      out_lo = H.hshots[it.shot].lo[1 - P.parity];
+    }
     const int kbeg = it.z0 - kRadius;
     const int kend = it.z1 + kRadius;
     const int gx = it.x0 + lx;
@@ -256,7 +305,7 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
           // FP32 pairs).  The source cell then gains the step's source
           // (original/OpenMP/openmp_insertsource.c:7-13), added by the
           // thread that decoded it.
-          const float inv = exp2i(-H.e_cur[k]);
+          const float inv = exp2i(-e_cur[k]);
           const uint2 *hv2 = reinterpret_cast<const uint2 *>(st);
           const unsigned *rv2 = reinterpret_cast<const unsigned *>(st + G::OFF_LO);
           float4 *Hs4 = reinterpret_cast<float4 *>(Hs);
@@ -289,18 +338,21 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
           produce();
         }
         if (tid == 0 && *s_pend >= 0) {
-          const int pend_z = *s_pend;
+          const int pend_z = *s_pend, ps = *s_pend_shot;
           const unsigned v = smax[sel ^ 1];
           smax[sel ^ 1] = 0u;
           if (v) {
-            atomicMax(&H.m_new[pend_z], v);
+            atomicMax(&m_new_of(ps)[pend_z], v);
             // Beyond FP16's range: the scale bound was exceeded.
-            if (!(__fmul_rn(__uint_as_float(v), exp2i(H.e_new[pend_z])) < 65504.0f)) atomicOr(P.err, 4u);
+            if (!(__fmul_rn(__uint_as_float(v), exp2i(e_new_of(ps)[pend_z])) < 65504.0f)) atomicOr(P.err, 4u);
           }
         }
         const bool center = (k >= it.z0) && (k < it.z1);
         const bool upd = (k - kRadius >= it.z0);
-        if (tid == 0) *s_pend = upd ? k - kRadius : -1;
+        if (tid == 0) {
+          *s_pend = upd ? k - kRadius : -1;
+          *s_pend_shot = it.shot;
+        }
 
         const f2 c = Hs[hc];
         f2 xa[4], xb[4], ya[4], yb[4];
@@ -368,19 +420,19 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
           const unsigned phv = reinterpret_cast<const unsigned *>(st + G::OFF_PHI)[ci];
           unsigned short prv = 0;
           if constexpr (EXT) prv = reinterpret_cast<const unsigned short *>(st + G::OFF_PLO)[ly * G::HX + lx + kRadius];
-          f2 old = decode<EXT>(phv, prv, exp2i(-H.e_prev[zc]));
+          f2 old = decode<EXT>(phv, prv, exp2i(-e_prev[zc]));
           if (zc == cor_z) {
             if (gx == sd.cor_x && gy == sd.cor_y) old = add2(old, splat(P.cor));
           }
           const f2 curv = Pr[cs];
           const f2 nw = fma2(mk2(rhsp, rhsq), splat(P.dt2), sub2(add2(curv, curv), old));
-          const float scl = exp2i(H.e_new[zc]);
+          const float scl = exp2i(e_new[zc]);
           unsigned ohv;
           unsigned short orv;
           encode<EXT>(nw, scl, ohv, orv);
           if (valid) {
-            H.out_hi[(long)zc * plane + oidx] = ohv;
-            if constexpr (EXT) H.out_lo[(long)zc * plane + oidx] = orv;
+            out_hi[(long)zc * plane + oidx] = ohv;
+            if constexpr (EXT) out_lo[(long)zc * plane + oidx] = orv;
           }
           // The warp's largest magnitude: the bits of non-negative floats
           // order like the floats, so one integer warp reduction finds it
@@ -418,11 +470,11 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
   // The last plane's CTA maximum.
   if (__syncthreads_or(bad)) goto aborted;
   if (tid == 0 && *s_pend >= 0) {
-    const int pend_z = *s_pend;
+    const int pend_z = *s_pend, ps = *s_pend_shot;
     const unsigned v = smax[sel ^ 1];
     if (v) {
-      atomicMax(&H.m_new[pend_z], v);
-      if (!(__fmul_rn(__uint_as_float(v), exp2i(H.e_new[pend_z])) < 65504.0f)) atomicOr(P.err, 4u);
+      atomicMax(&m_new_of(ps)[pend_z], v);
+      if (!(__fmul_rn(__uint_as_float(v), exp2i(e_new_of(ps)[pend_z])) < 65504.0f)) atomicOr(P.err, 4u);
     }
   }
   return;
@@ -526,22 +578,37 @@ __global__ void k_half_decode(const unsigned *__restrict__ hv, const unsigned sh
 
 #define FLT_HALF_SHAPES(X) X(12, 4) X(12, 5) X(12, 6) X(8, 6) X(16, 4) X(16, 5)
 
-template <int TY, int S, bool EXT>
-static cudaError_t launch_half_t(const HalfLaunch &L, cudaStream_t s) {
+// Dynamic shared-memory limit of a kernel shape (once; outside any stream
+// capture before a captured launch).
+template <int TY, int S, bool EXT, bool BATCH>
+static cudaError_t prepare_half_t() {
   constexpr size_t smem = smem_bytes_half<TY, S, EXT>();
   static bool ready = false;
   if (!ready) {
-    cudaError_t e = cudaFuncSetAttribute(k_propagate_half<TY, S, true, EXT>,
+    cudaError_t e = cudaFuncSetAttribute(k_propagate_half<TY, S, true, EXT, BATCH>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_propagate_half<TY, S, false, EXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem);
+      e = cudaFuncSetAttribute(k_propagate_half<TY, S, false, EXT, BATCH>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     ready = true;
   }
-  auto kern = L.h.p.iso ? k_propagate_half<TY, S, true, EXT> : k_propagate_half<TY, S, false, EXT>;
+  return cudaSuccess;
+}
+
+template <int TY, int S, bool EXT, bool BATCH>
+static cudaError_t launch_half_t(const HalfLaunch &L, cudaStream_t s) {
+  constexpr size_t smem = smem_bytes_half<TY, S, EXT>();
+  const cudaError_t e = prepare_half_t<TY, S, EXT, BATCH>();
+  if (e != cudaSuccess) return e;
+  auto kern = L.h.p.iso ? k_propagate_half<TY, S, true, EXT, BATCH> : k_propagate_half<TY, S, false, EXT, BATCH>;
   kern<<<L.grid, kTileX * TY, smem, s>>>(L.m, L.h);
   return cudaGetLastError();
+}
+
+template <int TY, int S, bool EXT>
+static cudaError_t launch_half_b(const HalfLaunch &L, cudaStream_t s) {
+  return L.batch ? launch_half_t<TY, S, EXT, true>(L, s) : launch_half_t<TY, S, EXT, false>(L, s);
 }
 
 bool propagate_half_supported(int tile_rows, int stages) {
@@ -555,7 +622,17 @@ bool propagate_half_supported(int tile_rows, int stages) {
 cudaError_t propagate_half_launch(const HalfLaunch &L, bool ext, cudaStream_t s) {
 #define X(a, b)                          \
   if (L.tile_rows == a && L.stages == b) \
-    return ext ? launch_half_t<a, b, true>(L, s) : launch_half_t<a, b, false>(L, s);
+    return ext ? launch_half_b<a, b, true>(L, s) : launch_half_b<a, b, false>(L, s);
+  FLT_HALF_SHAPES(X)
+#undef X
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t propagate_half_prepare(int tile_rows, int stages, bool ext, bool batch) {
+#define X(a, b)                                                                                  \
+  if (tile_rows == a && stages == b)                                                             \
+    return ext ? (batch ? prepare_half_t<a, b, true, true>() : prepare_half_t<a, b, true, false>()) \
+               : (batch ? prepare_half_t<a, b, false, true>() : prepare_half_t<a, b, false, false>());
   FLT_HALF_SHAPES(X)
 #undef X
   return cudaErrorInvalidValue;
@@ -564,6 +641,38 @@ cudaError_t propagate_half_launch(const HalfLaunch &L, bool ext, cudaStream_t s)
 cudaError_t half_scales(const unsigned *m_cur, unsigned *m_prev, int *e_new, int sz, int src_z, float src_abs,
                         cudaStream_t s) {
   k_half_scales<<<(sz + 127) / 128, 128, 0, s>>>(m_cur, m_prev, e_new, sz, src_z, src_abs);
+  return cudaGetLastError();
+}
+
+// The same for every running shot of a batch (block i: shot order[i]); the
+// current field is in buffer c and uses exponent slot ecur.
+__global__ void k_half_scales_batch(const HalfShot *__restrict__ hs, const ShotDesc *__restrict__ sd,
+                                    const int *__restrict__ order, int c, int ecur, float src_abs) {
+  const int shot = order[blockIdx.x];
+  const int sz = sd[shot].sz, src_z = sd[shot].src_z;
+  const unsigned *m_cur = hs[shot].Mx + c * sz;
+  unsigned *m_prev = hs[shot].Mx + (1 - c) * sz;
+  int *e_new = hs[shot].E + ((ecur + 1) % 3) * sz;
+  for (int z = threadIdx.x; z < sz; z += blockDim.x) {
+    float b = 0.0f;
+    for (int dz = -kRadius; dz <= kRadius; ++dz)
+      if (z + dz >= 0 && z + dz < sz) b = fmaxf(b, __uint_as_float(m_cur[z + dz]));
+    b = 4.0f * b + __uint_as_float(m_prev[z]);
+    if (abs(z - src_z) <= kRadius) b += 4.0f * src_abs;
+    int e = 0;
+    if (b > 0.0f) {
+      int ex;
+      frexpf(b, &ex);
+      e = min(max(14 - ex, -100), 100);
+    }
+    e_new[z] = e;
+    m_prev[z] = 0u;
+  }
+}
+
+cudaError_t half_scales_batch(const HalfShot *hs, const ShotDesc *sd, const int *order, int active, int c, int ecur,
+                              float src_abs, cudaStream_t s) {
+  k_half_scales_batch<<<active, 256, 0, s>>>(hs, sd, order, c, ecur, src_abs);
   return cudaGetLastError();
 }
 

@@ -218,7 +218,10 @@ int FLETCHER_DumpSliceSummary(int sx, int sy, int sz, const FletcherSlice *slice
  * model, source cell (inside the updated region) and step count.  The
  * single-shot state of part 1 is separate and unaffected. */
 
-/* Starts an empty batch (frees a previous one). */
+/* Starts an empty batch (frees a previous one).  Every shot of the batch
+ * is stored in the form FLETCHER_SetForm last selected (FP32, FP16 or
+ * FP16X; 16-bit forms take two launches per step: the plane scales of all
+ * running shots, then the step). */
 int FLETCHER_BatchCreate(int bord, float dx, float dy, float dz, float dt);
 /* Adds a shot: grid sx*sy*sz, model = vpz vsv epsilon delta phi theta
  * (sx*sy*sz floats each, consecutive, boundary already applied), source

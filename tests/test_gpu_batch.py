@@ -4,7 +4,10 @@ graph time loop) against single-shot runs of the same shots and the oracle.
 The batched kernel evaluates every cell with the same operations as the
 single-shot kernel, so each shot's fields must be bit-identical to its own
 single-shot run, whatever the other shots in the batch and whether the loop
-runs from a CUDA graph; the oracle bounds them at relative L2 1e-5."""
+runs from a CUDA graph; the oracle bounds them at relative L2 1e-5.  The
+same holds for the 16-bit storage forms: a shot's per-plane scales depend
+only on its own field's maxima, so a batched FP16 or FP16X shot is
+bit-identical to its single-shot run in that form."""
 import numpy as np
 import pytest
 
@@ -25,8 +28,8 @@ def rel_l2(a, b):
     return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(np.asarray(b, np.float64)))
 
 
-def single(prob, model):
-    prop = Propagator()
+def single(prob, model, form="fp32"):
+    prop = Propagator(form=form)
     prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model)
     prop.run(prob.steps, prob.i_source, prob.sources())
     prop.synchronize()
@@ -78,3 +81,28 @@ def test_batch_tile_shapes_and_rerun_identical():
     batch.close()
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("form", ["fp16", "fp16x"])
+def test_half_batch_matches_single_shot_runs(form):
+    models = [p.model() for p in SHOTS]
+    batch = Batch(form=form)
+    for p, m in zip(SHOTS, models):
+        batch.add(p, m)
+    batch.run()
+    got = [[batch.field(i, k) for k in range(4)] for i in range(len(SHOTS))]
+    info = batch.info()
+    # Another tile shape and the loop without a graph give the same fields.
+    batch.reset()
+    batch.set_tile(12, 5)
+    batch.run(use_graph=False)
+    again = [batch.field(i, 0) for i in range(len(SHOTS))]
+    batch.close()
+    # Two launches per step: the plane scales of every running shot, then the step.
+    assert info["launches"] == 2 * max(p.steps for p in SHOTS)
+    for i, (p, m) in enumerate(zip(SHOTS, models)):
+        ref = single(p, m, form)
+        assert np.abs(ref[0]).max() > 0.0
+        for k in range(4):
+            assert np.array_equal(got[i][k], ref[k]), (form, i, k)
+        assert np.array_equal(again[i], ref[0]), (form, i)
