@@ -780,6 +780,8 @@ int step() {
     const float sabs = fabsf(P.src) + fabsf(P.cor);
     CK(half_scales(g.Mx + c * sz, g.Mx + p * sz, g.E + enew * sz, sz, sz_src, sabs, g_stream));
     HalfLaunch HL;
+    memset(&HL, 0, sizeof(HL));
+    HL.batch = false;
     HL.h.p = P;
     HL.h.p.seg = g.seg;  // the 16-bit kernel always walks the segment list
     HL.h.p.nitems = g.nseg;

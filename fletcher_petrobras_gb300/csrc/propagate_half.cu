@@ -620,6 +620,10 @@ bool propagate_half_supported(int tile_rows, int stages) {
 }
 
 cudaError_t propagate_half_launch(const HalfLaunch &L, bool ext, cudaStream_t s) {
+  // The work description the chosen kernel reads must be present.
+  if (L.batch ? (!L.h.p.items || !L.h.p.shots || !L.h.hshots || !L.h.hmaps)
+              : (!L.h.p.seg || !L.h.p.cta_first || !L.h.out_hi || !L.h.e_cur))
+    return cudaErrorInvalidValue;
 #define X(a, b)                          \
   if (L.tile_rows == a && L.stages == b) \
     return ext ? launch_half_b<a, b, true>(L, s) : launch_half_b<a, b, false>(L, s);
