@@ -105,7 +105,7 @@ struct HalfShot {
 };
 
 // A batched shot's tensor maps, by the buffer that holds the current field.
-struct alignas(64) HalfShotMaps {
+struct HalfShotMaps {
   HalfMaps m[2];
 };
 
