@@ -125,30 +125,33 @@ __device__ __forceinline__ void encode(f2 v, float sc, unsigned &hv, unsigned sh
 
 struct HItem {
   int x0, y0, z0, z1;
+};
+
+// Segment `item` of the launch's list: {x0, y0, z0, z1}.
+__device__ __forceinline__ HItem decode_hitem(int item, const PropParams &P) {
+  const int4 w = P.seg[item];
+  HItem it;
+  it.x0 = w.x;
+  it.y0 = w.y;
+  it.z0 = w.z;
+  it.z1 = w.w;
+  return it;
+}
+
+// A batched work item {shot, x0, y0, chunk index} as a z range of one shot.
+struct BItem : HItem {
   int shot;
 };
 
-// Item `item` of the launch: a segment {x0, y0, z0, z1} of the single shot's
-// list, or (batched) a work item {shot, x0, y0, chunk index}.
-template <bool BATCH>
-__device__ __forceinline__ HItem decode_hitem(int item, const PropParams &P) {
-  HItem it;
-  if constexpr (BATCH) {
-    const int4 w = P.items[item];
-    const ShotDesc &d = P.shots[w.x];
-    it.x0 = w.y;
-    it.y0 = w.z;
-    it.z0 = d.bord + w.w * d.chunk;
-    it.z1 = min(it.z0 + d.chunk, d.sz - d.bord);
-    it.shot = w.x;
-  } else {
-    const int4 w = P.seg[item];
-    it.x0 = w.x;
-    it.y0 = w.y;
-    it.z0 = w.z;
-    it.z1 = w.w;
-    it.shot = 0;
-  }
+__device__ __forceinline__ BItem decode_bitem(int item, const PropParams &P) {
+  const int4 w = P.items[item];
+  const ShotDesc &d = P.shots[w.x];
+  BItem it;
+  it.x0 = w.y;
+  it.y0 = w.z;
+  it.z0 = d.bord + w.w * d.chunk;
+  it.z1 = min(it.z0 + d.chunk, d.sz - d.bord);
+  it.shot = w.x;
   return it;
 }
 
@@ -175,11 +178,12 @@ __device__ __forceinline__ void issue_half(unsigned char *stage, uint64_t *bar, 
   }
 }
 
-template <int TY, int S, bool ISO, bool EXT, bool BATCH>
+template <int TY, int S, bool ISO, bool EXT>
 __global__ void __launch_bounds__(kTileX *TY, 1)
     k_propagate_half(const __grid_constant__ HalfMaps M, const __grid_constant__ HalfParams H) {
   using G = GeoH<TY, EXT>;
   const PropParams &P = H.p;
+  const ShotDesc &sd = P.one;
   constexpr int NTH = kTileX * TY;
   extern __shared__ unsigned char smem_dyn[];
   unsigned char *smem = smem_dyn + ((128u - (smem_addr(smem_dyn) & 127u)) & 127u);
@@ -194,25 +198,312 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
   volatile int *s_end = ctl + 3;                           // end of this CTA's segments
   unsigned *smax = reinterpret_cast<unsigned *>(ctl + 4);  // CTA max of the plane updated, by step parity
   volatile int *s_pend = ctl + 6;  // plane whose CTA maximum waits in smax[sel ^ 1] (-1: none)
-  volatile int *s_pend_shot = ctl + 7;  // and its shot (batched launches)
-  HRec *rec = reinterpret_cast<HRec *>(ctl + 8);  // batched: records of this and the next item
 
   const int tid = threadIdx.x;
   const int lx = tid & 31;
   const int ly = tid >> 5;
-  // This CTA's items: its segments cta_first[b] .. cta_first[b + 1] - 1,
-  // or (batched) items b, b + grid, ... below nitems.  The end and thread
-  // 0's pending plane live in shared memory (no loop registers).
-  const int item_first = BATCH ? (int)blockIdx.x : P.cta_first[blockIdx.x];
-  if (item_first >= (BATCH ? P.nitems : P.cta_first[blockIdx.x + 1])) return;
-  auto item_end = [&]() { return BATCH ? P.nitems : *s_end; };
-  auto item_step = [&]() { return BATCH ? (int)gridDim.x : 1; };
-  // Tensor maps of an item: the shot's (batched) or the launch's.
-  auto maps_of = [&](const HItem &it) -> const HalfMaps & {
-    if constexpr (BATCH) return H.hmaps[it.shot].m[P.parity];
-    else return M;
+  // This CTA's segments: cta_first[b] .. cta_first[b + 1] - 1.  The end
+  // and thread 0's pending plane live in shared memory (no loop registers).
+  const int item_first = P.cta_first[blockIdx.x];
+  if (item_first >= P.cta_first[blockIdx.x + 1]) return;
+  auto item_end = [&]() { return *s_end; };
+  const bool producer = tid == (TY - 1) * 32;
+  auto produce = [&]() {
+    int item = cur[0], k = cur[1], stg = cur[2];
+    const HItem it = decode_hitem(item, P);
+    issue_half<TY, EXT>(smem + stg * G::STAGE_B, &full[stg], it, k, M);
+    if (++stg == S) stg = 0;
+    if (++k >= it.z1 + kRadius) {
+      ++item;
+      if (item < item_end()) k = decode_hitem(item, P).z0 - kRadius;
+    }
+    cur[0] = item;
+    cur[1] = k;
+    cur[2] = stg;
   };
-  // Batched: thread 0 fills the record of an item.  The record of a CTA's
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
+    mbar_init(xchg, TY);
+    mbar_fence_init();
+    cur[0] = item_first;
+    cur[1] = decode_hitem(item_first, P).z0 - kRadius;
+    cur[2] = 0;
+    *s_end = P.cta_first[blockIdx.x + 1];
+    *s_pend = -1;
+    smax[0] = smax[1] = 0u;
+  }
+  __syncthreads();
+  if (producer) {
+    tma_prefetch_desc(&M.cur_hi);
+    tma_prefetch_desc(&M.prev_hi);
+    tma_prefetch_desc(&M.arr);
+    tma_prefetch_desc(&M.upd);
+    // Prologue: S-1 steps; afterwards each step refills the stage freed by
+    // the step before it.
+    for (int a = 0; a < S - 1 && cur[0] < item_end(); ++a) produce();
+  }
+
+  const float sx1 = P.inv_dx, sy1 = P.inv_dy, sz1 = P.inv_dz;
+  const float sxx = P.inv_dxx, syy = P.inv_dyy, szz = P.inv_dzz;
+  const bool halo_warp = ly < TY / 4;
+  const int hr = ly * 4 + (lx >> 3);
+  const int hxc = (lx & 7) < 4 ? (lx & 7) : G::TX + (lx & 7);
+  const int hh = (hr + kRadius) * G::HX + hxc;
+  const long plane = (long)sd.pitch * sd.sy;
+
+  int stage = 0;
+  uint32_t phase = 0, xphase = 0;
+  int sel = 0;
+  int abw = 0;  // shared A/B ring slot of the arriving plane (the plane 4 back is at abw + 1)
+  bool bad = false;
+  for (int item = item_first; item < item_end(); ++item) {
+    const HItem it = decode_hitem(item, P);
+    const int kbeg = it.z0 - kRadius;
+    const int kend = it.z1 + kRadius;
+    const int gx = it.x0 + lx;
+    const int gy = it.y0 + ly;
+    const bool valid = (gx >= sd.bord) && (gx < sd.sx - sd.bord) && (gy >= sd.bord) && (gy < sd.sy - sd.bord);
+    const long oidx = (long)gy * sd.pitch + gx;
+    const int ci = ly * G::TX + lx;
+    const int hc = (ly + kRadius) * G::HX + (lx + kRadius);
+    const int src_z = sd.src_z, cor_z = sd.cor_z;
+
+    f2 Pr[9], Dx[9], Dy[9], A[9], B[9];
+
+    for (int kb = kbeg; kb < kend; kb += 9) {
+#pragma unroll
+      for (int j = 0; j < 9; ++j) {
+        const int k = kb + j;
+        if (k >= kend) break;
+        unsigned char *st = smem + stage * G::STAGE_B;
+        bad |= !mbar_wait(&full[stage], phase, kWaitLimitNs);
+        f2 *Hs = H32 + sel * G::HXY;
+        {
+          // Decode the arriving plane once per cell, two cells per thread
+          // (one 64-bit load of two half2 cells, one 128-bit store of their
+          // FP32 pairs).  The source cell then gains the step's source
+          // (original/OpenMP/openmp_insertsource.c:7-13), added by the
+          // thread that decoded it.
+          const float inv = exp2i(-H.e_cur[k]);
+          const uint2 *hv2 = reinterpret_cast<const uint2 *>(st);
+          const unsigned *rv2 = reinterpret_cast<const unsigned *>(st + G::OFF_LO);
+          float4 *Hs4 = reinterpret_cast<float4 *>(Hs);
+#pragma unroll
+          for (int c0 = 0; c0 < G::HXY / 2; c0 += NTH) {
+            const int c2 = c0 + tid;
+            if (c2 < G::HXY / 2) {
+              const uint2 h = hv2[c2];
+              const unsigned r = EXT ? rv2[c2] : 0u;
+              const f2 a = decode<EXT>(h.x, (unsigned short)(r & 0xffffu), inv);
+              const f2 b = decode<EXT>(h.y, (unsigned short)(r >> 16), inv);
+              Hs4[c2] = make_float4(lo(a), hi(a), lo(b), hi(b));
+            }
+          }
+          if (k == src_z) {
+            // Halo-tile index of the source cell, if it lies in this tile.
+            const int rx = sd.src_x - (it.x0 - kRadius), ry = sd.src_y - (it.y0 - kRadius);
+            if (rx >= 0 && rx < G::HX && ry >= 0 && ry < G::HY) {
+              const int src_c = ry * G::HX + rx;
+              if (tid == (src_c >> 1) % NTH) Hs[src_c] = add2(Hs[src_c], splat(P.src));
+            }
+          }
+        }
+        // Every thread is past the previous step: its stage is free and the
+        // CTA maximum of the plane it updated is complete.  Every thread
+        // takes the same branch (a wait that gave up anywhere ends the CTA).
+        if (__syncthreads_or(bad)) goto aborted;
+        if (producer && cur[0] < item_end()) {
+          fence_proxy_async_smem();
+          produce();
+        }
+        if (tid == 0 && *s_pend >= 0) {
+          const int pend_z = *s_pend;
+          const unsigned v = smax[sel ^ 1];
+          smax[sel ^ 1] = 0u;
+          if (v) {
+            atomicMax(&H.m_new[pend_z], v);
+            // Beyond FP16's range: the scale bound was exceeded.
+            if (!(__fmul_rn(__uint_as_float(v), exp2i(H.e_new[pend_z])) < 65504.0f)) atomicOr(P.err, 4u);
+          }
+        }
+        const bool center = (k >= it.z0) && (k < it.z1);
+        const bool upd = (k - kRadius >= it.z0);
+        if (tid == 0) *s_pend = upd ? k - kRadius : -1;
+
+        const f2 c = Hs[hc];
+        f2 xa[4], xb[4], ya[4], yb[4];
+#pragma unroll
+        for (int o = 1; o <= 4; ++o) {
+          xa[o - 1] = Hs[hc + o];
+          xb[o - 1] = Hs[hc - o];
+          ya[o - 1] = Hs[hc + o * G::HX];
+          yb[o - 1] = Hs[hc - o * G::HX];
+        }
+        const f2 d1x = scale<ISO>(d1(xa[0], xb[0], xa[1], xb[1], xa[2], xb[2], xa[3], xb[3]), sx1);
+        const f2 d1y = scale<ISO>(d1(ya[0], yb[0], ya[1], yb[1], ya[2], yb[2], ya[3], yb[3]), sy1);
+        Pr[j] = c;
+        Dx[j] = d1x;
+        Dy[j] = d1y;
+        f2 d2x, d2y;
+        f2 *db = dbuf + sel * (TY * G::HX);
+        if (center) {
+          d2x = scale<ISO>(d2(c, xa[0], xb[0], xa[1], xb[1], xa[2], xb[2], xa[3], xb[3]), sxx);
+          d2y = scale<ISO>(d2(c, ya[0], yb[0], ya[1], yb[1], ya[2], yb[2], ya[3], yb[3]), syy);
+          db[ly * G::HX + lx + kRadius] = d1y;
+          if (halo_warp) {
+            f2 ha[4], hb[4];
+#pragma unroll
+            for (int o = 1; o <= 4; ++o) {
+              ha[o - 1] = Hs[hh + o * G::HX];
+              hb[o - 1] = Hs[hh - o * G::HX];
+            }
+            db[hr * G::HX + hxc] = scale<ISO>(d1(ha[0], hb[0], ha[1], hb[1], ha[2], hb[2], ha[3], hb[3]), sy1);
+          }
+        }
+        __syncwarp();
+        if (lx == 0) mbar_arrive(xchg);
+        if (upd) {
+          const int cs = (j + 5) % 9;
+#define RP(o) Pr[(cs + (o)) % 9]
+#define RX(o) Dx[(cs + (o)) % 9]
+#define RY(o) Dy[(cs + (o)) % 9]
+          const f2 d2z = scale<ISO>(d2(RP(0), RP(1), RP(8), RP(2), RP(7), RP(3), RP(6), RP(4), RP(5)), szz);
+          const f2 dxz = scale<ISO>(d1(RX(1), RX(8), RX(2), RX(7), RX(3), RX(6), RX(4), RX(5)), sz1);
+          const f2 dyz = scale<ISO>(d1(RY(1), RY(8), RY(2), RY(7), RY(3), RY(6), RY(4), RY(5)), sz1);
+#undef RP
+#undef RX
+#undef RY
+          const float *cu = reinterpret_cast<const float *>(st + G::OFF_UPD);
+          const float czz = cu[ci], cxz = cu[G::NT + ci], cyz = cu[2 * G::NT + ci];
+          const float v2px = cu[3 * G::NT + ci], v2pz = cu[4 * G::NT + ci];
+          const float v2sz = cu[5 * G::NT + ci], v2pn = cu[6 * G::NT + ci];
+          f2 Ak, Bk;
+          if constexpr (G::AB_SMEM) {
+            const float4 ab = ABs[(abw == 4 ? 0 : abw + 1) * G::NT + ci];
+            Ak = mk2(ab.x, ab.y);
+            Bk = mk2(ab.z, ab.w);
+          } else {
+            Ak = A[cs];
+            Bk = B[cs];
+          }
+          const f2 h1 = fma2(splat(cyz), dyz, fma2(splat(cxz), dxz, fma2(splat(czz), d2z, Ak)));
+          const f2 h2 = sub2(add2(Bk, d2z), h1);
+          const float h1p = lo(h1), h1q = hi(h1), h2p = lo(h2), h2q = hi(h2);
+          const float t = __fmul_rn(v2pz, h1q);
+          const float rhsp = __fmaf_rn(v2sz, __fsub_rn(h1p, h1q), __fmaf_rn(v2px, h2p, t));
+          const float rhsq = __fmaf_rn(-v2sz, __fsub_rn(h2p, h2q), __fmaf_rn(v2pn, h2p, t));
+          const int zc = k - kRadius;
+          const unsigned phv = reinterpret_cast<const unsigned *>(st + G::OFF_PHI)[ci];
+          unsigned short prv = 0;
+          if constexpr (EXT) prv = reinterpret_cast<const unsigned short *>(st + G::OFF_PLO)[ly * G::HX + lx + kRadius];
+          f2 old = decode<EXT>(phv, prv, exp2i(-H.e_prev[zc]));
+          if (zc == cor_z) {
+            if (gx == sd.cor_x && gy == sd.cor_y) old = add2(old, splat(P.cor));
+          }
+          const f2 curv = Pr[cs];
+          const f2 nw = fma2(mk2(rhsp, rhsq), splat(P.dt2), sub2(add2(curv, curv), old));
+          const float scl = exp2i(H.e_new[zc]);
+          unsigned ohv;
+          unsigned short orv;
+          encode<EXT>(nw, scl, ohv, orv);
+          if (valid) {
+            H.out_hi[(long)zc * plane + oidx] = ohv;
+            if constexpr (EXT) H.out_lo[(long)zc * plane + oidx] = orv;
+          }
+          // The warp's largest magnitude: the bits of non-negative floats
+          // order like the floats, so one integer warp reduction finds it
+          // (a NaN, above every finite value, reaches the range check).
+          unsigned mb = 0u;
+          if (valid) mb = max(__float_as_uint(fabsf(lo(nw))), __float_as_uint(fabsf(hi(nw))));
+          mb = __reduce_max_sync(0xffffffffu, mb);
+          if (lx == 0 && mb) atomicMax(&smax[sel], mb);
+        }
+        bad |= !mbar_wait(xchg, xphase, kWaitLimitNs);
+        xphase ^= 1u;
+        if (center) {
+          const f2 *dr = db + ly * G::HX + lx + kRadius;
+          const f2 dxy = scale<ISO>(d1(dr[1], dr[-1], dr[2], dr[-2], dr[3], dr[-3], dr[4], dr[-4]), sx1);
+          const float *ca = reinterpret_cast<const float *>(st + G::OFF_ARR);
+          const float cxx = ca[ci], cyy = ca[G::NT + ci], cxy = ca[2 * G::NT + ci];
+          const f2 av = fma2(splat(cxy), dxy, fma2(splat(cyy), d2y, mul2(splat(cxx), d2x)));
+          const f2 bv = add2(d2x, d2y);
+          if constexpr (G::AB_SMEM) {
+            ABs[abw * G::NT + ci] = make_float4(lo(av), hi(av), lo(bv), hi(bv));
+          } else {
+            A[j] = av;
+            B[j] = bv;
+          }
+        }
+        sel ^= 1;
+        abw = abw == 4 ? 0 : abw + 1;
+        if (++stage == S) {
+          stage = 0;
+          phase ^= 1u;
+        }
+      }
+    }
+  }
+  // The last plane's CTA maximum.
+  if (__syncthreads_or(bad)) goto aborted;
+  if (tid == 0 && *s_pend >= 0) {
+    const int pend_z = *s_pend;
+    const unsigned v = smax[sel ^ 1];
+    if (v) {
+      atomicMax(&H.m_new[pend_z], v);
+      if (!(__fmul_rn(__uint_as_float(v), exp2i(H.e_new[pend_z])) < 65504.0f)) atomicOr(P.err, 4u);
+    }
+  }
+  return;
+aborted:
+  // A bounded wait gave up (every thread of the CTA arrives here together,
+  // from a barrier).  Thread 0 waits, bounded, for the loads that may still
+  // be in flight into this CTA's stages.
+  if (tid == 0) {
+    atomicOr(P.err, 1u);
+    for (int a = 0; a < S; ++a) {
+      const int s2 = (stage + a) % S;
+      (void)mbar_wait(&full[s2], phase ^ uint32_t(stage + a >= S), kWaitLimitNs);
+    }
+  }
+}
+
+// The same step for a batch of shots (p.items, p.shots, hshots, hmaps): each
+// item is a z-chunk of one tile column of one shot, with that shot's tensor
+// maps, buffers and exponents.  It is a kernel of its own because folding
+// the batched lookups into k_propagate_half, even behind compile-time
+// switches, made the single-shot kernel 9-11% slower at 504^3.
+template <int TY, int S, bool ISO, bool EXT>
+__global__ void __launch_bounds__(kTileX *TY, 1)
+    k_propagate_half_batch(const __grid_constant__ HalfParams H) {
+  using G = GeoH<TY, EXT>;
+  const PropParams &P = H.p;
+  constexpr int NTH = kTileX * TY;
+  extern __shared__ unsigned char smem_dyn[];
+  unsigned char *smem = smem_dyn + ((128u - (smem_addr(smem_dyn) & 127u)) & 127u);
+  unsigned char *tail = smem + S * G::STAGE_B;
+  f2 *H32 = reinterpret_cast<f2 *>(tail + G::OFF_H32);
+  f2 *dbuf = reinterpret_cast<f2 *>(tail + G::OFF_DB);
+  float4 *ABs = reinterpret_cast<float4 *>(tail + G::OFF_AB);  // [5][NT] (AB_SMEM)
+  uint64_t *full = reinterpret_cast<uint64_t *>(tail + G::OFF_BAR);
+  uint64_t *xchg = full + S;
+  int *ctl = reinterpret_cast<int *>(xchg + 1);
+  int *cur = ctl;                                          // producer cursor: item, k, stage
+  unsigned *smax = reinterpret_cast<unsigned *>(ctl + 4);  // CTA max of the plane updated, by step parity
+  volatile int *s_pend = ctl + 6;  // plane whose CTA maximum waits in smax[sel ^ 1] (-1: none)
+  volatile int *s_pend_shot = ctl + 7;  // and its shot
+  HRec *rec = reinterpret_cast<HRec *>(ctl + 8);  // records of this CTA's current and next item
+
+  const int tid = threadIdx.x;
+  const int lx = tid & 31;
+  const int ly = tid >> 5;
+  // This CTA's items: b, b + grid, ... below nitems.
+  const int item_first = blockIdx.x;
+  if (item_first >= P.nitems) return;
+  auto item_end = [&]() { return P.nitems; };
+  auto item_step = [&]() { return (int)gridDim.x; };
+  // Tensor maps of an item's shot, for the buffer holding its current field.
+  auto maps_of = [&](const BItem &it) -> const HalfMaps & { return H.hmaps[it.shot].m[P.parity]; };
+  // Thread 0 fills the record of an item.  The record of a CTA's
   // first item is filled before the start barrier; that of its next item
   // once every thread has passed the first plane of the current one (so no
   // thread still reads the previous item's record, which it replaces).
@@ -232,12 +523,12 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
   const bool producer = tid == (TY - 1) * 32;
   auto produce = [&]() {
     int item = cur[0], k = cur[1], stg = cur[2];
-    const HItem it = decode_hitem<BATCH>(item, P);
+    const BItem it = decode_bitem(item, P);
     issue_half<TY, EXT>(smem + stg * G::STAGE_B, &full[stg], it, k, maps_of(it));
     if (++stg == S) stg = 0;
     if (++k >= it.z1 + kRadius) {
       item += item_step();
-      if (item < item_end()) k = decode_hitem<BATCH>(item, P).z0 - kRadius;
+      if (item < item_end()) k = decode_bitem(item, P).z0 - kRadius;
     }
     cur[0] = item;
     cur[1] = k;
@@ -248,40 +539,25 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
     mbar_init(xchg, TY);
     mbar_fence_init();
     cur[0] = item_first;
-    cur[1] = decode_hitem<BATCH>(item_first, P).z0 - kRadius;
+    cur[1] = decode_bitem(item_first, P).z0 - kRadius;
     cur[2] = 0;
-    if constexpr (!BATCH) *s_end = P.cta_first[blockIdx.x + 1];
     *s_pend = -1;
     *s_pend_shot = 0;
-    if constexpr (BATCH) fill_rec(rec, item_first);
+    fill_rec(rec, item_first);
     smax[0] = smax[1] = 0u;
   }
   __syncthreads();
   if (producer) {
-    if constexpr (!BATCH) {
-      tma_prefetch_desc(&M.cur_hi);
-      tma_prefetch_desc(&M.prev_hi);
-      tma_prefetch_desc(&M.arr);
-      tma_prefetch_desc(&M.upd);
-    }
     // Prologue: S-1 steps; afterwards each step refills the stage freed by
     // the step before it.
     for (int a = 0; a < S - 1 && cur[0] < item_end(); ++a) produce();
   }
-  // Exponents and maxima of the new field of a shot (batched: the shot's
-  // buffers, where the current field is in buffer parity and exponent slot
-  // ecur; otherwise the launch's own arrays).
-  auto e_slot = [&](int shot, int d) -> const int * {
-    return H.hshots[shot].E + ((H.ecur + d) % 3) * P.shots[shot].sz;
-  };
+  // Exponents and maxima of the new field of a shot: its buffers, where the
+  // current field is in buffer parity and exponent slot ecur.
   auto e_new_of = [&](int shot) -> const int * {
-    if constexpr (BATCH) return e_slot(shot, 1);
-    else return H.e_new;
+    return H.hshots[shot].E + ((H.ecur + 1) % 3) * P.shots[shot].sz;
   };
-  auto m_new_of = [&](int shot) -> unsigned * {
-    if constexpr (BATCH) return H.hshots[shot].Mx + (1 - P.parity) * P.shots[shot].sz;
-    else return H.m_new;
-  };
+  auto m_new_of = [&](int shot) -> unsigned * { return H.hshots[shot].Mx + (1 - P.parity) * P.shots[shot].sz; };
 
   const float sx1 = P.inv_dx, sy1 = P.inv_dy, sz1 = P.inv_dz;
   const float sxx = P.inv_dxx, syy = P.inv_dyy, szz = P.inv_dzz;
@@ -295,48 +571,13 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
   int sel = 0;
   int abw = 0;  // shared A/B ring slot of the arriving plane (the plane 4 back is at abw + 1)
   bool bad = false;
-  int nloc = 0;  // items this CTA has finished (batched: record slot nloc & 1)
+  int nloc = 0;  // items this CTA has finished (record slot nloc & 1)
   for (int item = item_first; item < item_end(); item += item_step(), ++nloc) {
-    const HItem it = decode_hitem<BATCH>(item, P);
-    // The item's shot: its descriptor, and the values the plane loop reads
-    // (batched: from the item's record at each use).
-    auto desc = [&]() -> const ShotDesc & {
-      if constexpr (BATCH) return P.shots[it.shot];
-      else return P.one;
-    };
+    const BItem it = decode_bitem(item, P);
+    // The item's shot: its descriptor (read where needed) and its record,
+    // read at each use.
+    const ShotDesc *sdp = P.shots + it.shot;
     const volatile HRec *vr = rec + (nloc & 1);
-    auto e_cur = [&]() -> const int * {
-      if constexpr (BATCH) return vr->e_cur;
-      else return H.e_cur;
-    };
-    auto e_prev = [&]() -> const int * {
-      if constexpr (BATCH) return vr->e_prev;
-      else return H.e_prev;
-    };
-    auto e_new = [&]() -> const int * {
-      if constexpr (BATCH) return vr->e_new;
-      else return H.e_new;
-    };
-    auto out_hi = [&]() -> unsigned * {
-      if constexpr (BATCH) return vr->out_hi;
-      else return H.out_hi;
-    };
-    auto out_lo = [&]() -> unsigned short * {
-      if constexpr (BATCH) return vr->out_lo;
-      else return H.out_lo;
-    };
-    auto plane = [&]() -> long {
-      if constexpr (BATCH) return vr->plane;
-      else return (long)P.one.pitch * P.one.sy;
-    };
-    auto src_z = [&]() -> int {
-      if constexpr (BATCH) return vr->src_z;
-      else return P.one.src_z;
-    };
-    auto cor_z = [&]() -> int {
-      if constexpr (BATCH) return vr->cor_z;
-      else return P.one.cor_z;
-    };
     const int kbeg = it.z0 - kRadius;
     const int kend = it.z1 + kRadius;
     const int gx = it.x0 + lx;
@@ -344,7 +585,7 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
     bool valid;
     long oidx;
     {
-      const ShotDesc &sd = desc();
+      const ShotDesc &sd = *sdp;
       valid = (gx >= sd.bord) && (gx < sd.sx - sd.bord) && (gy >= sd.bord) && (gy < sd.sy - sd.bord);
       oidx = (long)gy * sd.pitch + gx;
     }
@@ -367,7 +608,7 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
           // FP32 pairs).  The source cell then gains the step's source
           // (original/OpenMP/openmp_insertsource.c:7-13), added by the
           // thread that decoded it.
-          const float inv = exp2i(-e_cur()[k]);
+          const float inv = exp2i(-vr->e_cur[k]);
           const uint2 *hv2 = reinterpret_cast<const uint2 *>(st);
           const unsigned *rv2 = reinterpret_cast<const unsigned *>(st + G::OFF_LO);
           float4 *Hs4 = reinterpret_cast<float4 *>(Hs);
@@ -382,9 +623,9 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
               Hs4[c2] = make_float4(lo(a), hi(a), lo(b), hi(b));
             }
           }
-          if (k == src_z()) {
+          if (k == vr->src_z) {
             // Halo-tile index of the source cell, if it lies in this tile.
-            const int rx = desc().src_x - (it.x0 - kRadius), ry = desc().src_y - (it.y0 - kRadius);
+            const int rx = sdp->src_x - (it.x0 - kRadius), ry = sdp->src_y - (it.y0 - kRadius);
             if (rx >= 0 && rx < G::HX && ry >= 0 && ry < G::HY) {
               const int src_c = ry * G::HX + rx;
               if (tid == (src_c >> 1) % NTH) Hs[src_c] = add2(Hs[src_c], splat(P.src));
@@ -395,9 +636,7 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
         // CTA maximum of the plane it updated is complete.  Every thread
         // takes the same branch (a wait that gave up anywhere ends the CTA).
         if (__syncthreads_or(bad)) goto aborted;
-        if constexpr (BATCH) {
-          if (tid == 0 && k == kbeg && item + item_step() < item_end()) fill_rec(rec + ((nloc + 1) & 1), item + item_step());
-        }
+        if (tid == 0 && k == kbeg && item + item_step() < item_end()) fill_rec(rec + ((nloc + 1) & 1), item + item_step());
         if (producer && cur[0] < item_end()) {
           fence_proxy_async_smem();
           produce();
@@ -485,20 +724,20 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
           const unsigned phv = reinterpret_cast<const unsigned *>(st + G::OFF_PHI)[ci];
           unsigned short prv = 0;
           if constexpr (EXT) prv = reinterpret_cast<const unsigned short *>(st + G::OFF_PLO)[ly * G::HX + lx + kRadius];
-          f2 old = decode<EXT>(phv, prv, exp2i(-e_prev()[zc]));
-          if (zc == cor_z()) {
-            if (gx == desc().cor_x && gy == desc().cor_y) old = add2(old, splat(P.cor));
+          f2 old = decode<EXT>(phv, prv, exp2i(-vr->e_prev[zc]));
+          if (zc == vr->cor_z) {
+            if (gx == sdp->cor_x && gy == sdp->cor_y) old = add2(old, splat(P.cor));
           }
           const f2 curv = Pr[cs];
           const f2 nw = fma2(mk2(rhsp, rhsq), splat(P.dt2), sub2(add2(curv, curv), old));
-          const float scl = exp2i(e_new()[zc]);
+          const float scl = exp2i(vr->e_new[zc]);
           unsigned ohv;
           unsigned short orv;
           encode<EXT>(nw, scl, ohv, orv);
           if (valid) {
-            const long o = (long)zc * plane() + oidx;
-            out_hi()[o] = ohv;
-            if constexpr (EXT) out_lo()[o] = orv;
+            const long o = (long)zc * vr->plane + oidx;
+            vr->out_hi[o] = ohv;
+            if constexpr (EXT) vr->out_lo[o] = orv;
           }
           // The warp's largest magnitude: the bits of non-negative floats
           // order like the floats, so one integer warp reduction finds it
@@ -644,37 +883,44 @@ __global__ void k_half_decode(const unsigned *__restrict__ hv, const unsigned sh
 
 #define FLT_HALF_SHAPES(X) X(12, 4) X(12, 5) X(12, 6) X(8, 6) X(16, 4) X(16, 5)
 
-// Dynamic shared-memory limit of a kernel shape (once; outside any stream
-// capture before a captured launch).
+// Dynamic shared-memory limit of a kernel shape, single-shot or batched
+// (once; outside any stream capture before a captured launch).
 template <int TY, int S, bool EXT, bool BATCH>
 static cudaError_t prepare_half_t() {
-  constexpr size_t smem = smem_bytes_half<TY, S, EXT>();
+  constexpr int smem = (int)smem_bytes_half<TY, S, EXT>();
   static bool ready = false;
   if (!ready) {
-    cudaError_t e = cudaFuncSetAttribute(k_propagate_half<TY, S, true, EXT, BATCH>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_propagate_half<TY, S, false, EXT, BATCH>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e;
+    if constexpr (BATCH) {
+      e = cudaFuncSetAttribute(k_propagate_half_batch<TY, S, true, EXT>, a, smem);
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(k_propagate_half_batch<TY, S, false, EXT>, a, smem);
+    } else {
+      e = cudaFuncSetAttribute(k_propagate_half<TY, S, true, EXT>, a, smem);
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(k_propagate_half<TY, S, false, EXT>, a, smem);
+    }
     if (e != cudaSuccess) return e;
     ready = true;
   }
   return cudaSuccess;
 }
 
-template <int TY, int S, bool EXT, bool BATCH>
-static cudaError_t launch_half_t(const HalfLaunch &L, cudaStream_t s) {
-  constexpr size_t smem = smem_bytes_half<TY, S, EXT>();
-  const cudaError_t e = prepare_half_t<TY, S, EXT, BATCH>();
-  if (e != cudaSuccess) return e;
-  auto kern = L.h.p.iso ? k_propagate_half<TY, S, true, EXT, BATCH> : k_propagate_half<TY, S, false, EXT, BATCH>;
-  kern<<<L.grid, kTileX * TY, smem, s>>>(L.m, L.h);
-  return cudaGetLastError();
-}
-
 template <int TY, int S, bool EXT>
 static cudaError_t launch_half_b(const HalfLaunch &L, cudaStream_t s) {
-  return L.batch ? launch_half_t<TY, S, EXT, true>(L, s) : launch_half_t<TY, S, EXT, false>(L, s);
+  constexpr size_t smem = smem_bytes_half<TY, S, EXT>();
+  const bool iso = L.h.p.iso;
+  if (L.batch) {
+    const cudaError_t e = prepare_half_t<TY, S, EXT, true>();
+    if (e != cudaSuccess) return e;
+    auto kern = iso ? k_propagate_half_batch<TY, S, true, EXT> : k_propagate_half_batch<TY, S, false, EXT>;
+    kern<<<L.grid, kTileX * TY, smem, s>>>(L.h);
+  } else {
+    const cudaError_t e = prepare_half_t<TY, S, EXT, false>();
+    if (e != cudaSuccess) return e;
+    auto kern = iso ? k_propagate_half<TY, S, true, EXT> : k_propagate_half<TY, S, false, EXT>;
+    kern<<<L.grid, kTileX * TY, smem, s>>>(L.m, L.h);
+  }
+  return cudaGetLastError();
 }
 
 bool propagate_half_supported(int tile_rows, int stages) {
