@@ -266,6 +266,8 @@ def run_gb300(args, ws, rank, local, group):
         if rc:
             raise RuntimeError("FLETCHER_Model failed: " + lib.FLETCHER_GetLastErrorString().decode())
         lib.FLETCHER_SetForm(FORMS["fp32"])
+        phases = (C.c_double * 4)()
+        lib.FLETCHER_ModelPhases(phases)
         e2e_wall = group.reduce(stats[2], "max")
         e2e = ws * cells * K / e2e_wall / 1e6
         del f
@@ -301,6 +303,8 @@ def run_gb300(args, ws, rank, local, group):
         "e2e": None if e2e is None else {
                 "value": round(e2e, 1), "unit": UNIT, "h2d_bytes_per_step": int(stats[3] / K),
                 "d2h_bytes_per_step": int(stats[4] / K), "wall_s": round(e2e_wall, 3),
+                "phases_s": {"setup": round(phases[0], 3), "steps": round(phases[1], 3),
+                             "snapshot_drain": round(phases[2], 3), "readback_finalize": round(phases[3], 3)},
                 "what": "FLETCHER_Model via the C ABI: DRIVER_Initialize (H2D of 6 model + 4 field arrays, "
                         "FP64 coefficient precompute) + K x (InsertSource, Propagate) + D2H snapshot of p every "
                         "0.01 s simulated + final D2H of p,q"},

@@ -54,6 +54,7 @@ SIGNATURES = {
                        + [FP] * 10 + [DP]),
     "FLETCHER_Autotune": (C.c_int, [C.c_char_p, C.c_int]),
     "FLETCHER_GetTileConfig": (C.c_int, [IP, IP]),
+    "FLETCHER_ModelPhases": (None, [DP]),
     "FLETCHER_TuneConfigLookup": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_int, IP, IP]),
     "FLETCHER_TuneConfigStore": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int]),
     "FLETCHER_SnapshotBegin": (C.c_int, [C.c_int, FP]),

@@ -319,6 +319,11 @@ int FLETCHER_Model(int st, long iSource, double fcut, float dt_output, int sx, i
                    int bord, float dx, float dy, float dz, float dt, float *pp, float *pc,
                    float *qp, float *qc, float *vpz, float *vsv, float *epsilon, float *delta,
                    float *phi, float *theta, double *stats);
+/* Wall seconds of the last FLETCHER_Model call by phase: phases[0] set-up
+ * (DRIVER_Initialize, page-locking the snapshot arrays), [1] the time loop,
+ * [2] waiting for the last snapshots, [3] final read-back and
+ * DRIVER_Finalize. */
+void FLETCHER_ModelPhases(double *phases);
 
 /* ===== Part 4: learned absorbing boundary (no counterpart in the reference,
  * whose absorbing zone is the random-velocity shell of original/boundary.c).
