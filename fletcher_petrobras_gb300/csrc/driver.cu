@@ -419,6 +419,35 @@ void free_state() {
   g = State();
 }
 
+// Page-locks caller arrays for the duration of copies between them and the
+// device: from or to pageable memory the driver stages a copy through its
+// own buffers at a fraction of the link's speed (on GB300 about 10 GB/s,
+// against a few ms per GB to lock and unlock).  An array that cannot be
+// locked (already locked, or not lockable) is copied as it is.  Unlocked,
+// after the stream's copies, when the object goes out of scope.
+struct HostPins {
+  void *p[10] = {};
+  int n = 0;
+  // `dest`: the device writes the array (read-back); otherwise it only reads it.
+  void add(const void *a, size_t bytes, bool dest = false) {
+    if (!a || !bytes || n == 10) return;
+    void *q = const_cast<void *>(a);
+    if (dest || cudaHostRegister(q, bytes, cudaHostRegisterReadOnly) != cudaSuccess) {
+      cudaGetLastError();
+      if (cudaHostRegister(q, bytes, cudaHostRegisterDefault) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+      }
+    }
+    p[n++] = q;
+  }
+  ~HostPins() {
+    if (n && g_stream) cudaStreamSynchronize(g_stream);
+    for (int k = 0; k < n; ++k) cudaHostUnregister(p[k]);
+    cudaGetLastError();
+  }
+};
+
 int ensure_stream() {
   if (!g_stream) {
     CK(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
@@ -633,10 +662,13 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   float *raw = nullptr;
   const float *src6[6] = {vpz, vsv, epsilon, delta, phi, theta};
   Raw6 r6;
+  HostPins pins;
   if (g.hostmem) {
     for (int k = 0; k < 6; ++k) r6.a[k] = src6[k];
   } else {
     CK(cudaMalloc(&raw, 6 * g.n * sizeof(float)));
+    for (int k = 0; k < 6; ++k) pins.add(src6[k], g.n * sizeof(float));
+    for (const float *f : {pp, pc, qp, qc}) pins.add(f, g.n * sizeof(float));
     for (int k = 0; k < 6; ++k) {
       CK(cudaMemcpyAsync(raw + k * g.n, src6[k], g.n * sizeof(float), cudaMemcpyHostToDevice, s));
       r6.a[k] = raw + k * g.n;
@@ -819,6 +851,8 @@ int read_component(int buf, int comp, float *host) {
   // Where the GPU writes host memory directly, the kernel writes the
   // caller's array; otherwise it goes through `scratch` and a copy.
   float *out = g.hostmem ? host : g.scratch;
+  HostPins pin;
+  if (!g.hostmem) pin.add(host, g.n * sizeof(float), true);
   if (half_form()) {
     const int slot = buf == g.cur ? g.ecur : (g.ecur + 2) % 3;
     CK(half_decode(g.Hh[buf], g.Hl[buf], g.E + slot * g.sz, out, comp, g.sx, g.sy, g.sz, g.pitch,
@@ -1432,6 +1466,8 @@ extern "C" int FLETCHER_BatchAddShot(int sx, int sy, int sz, const float *model,
     cudaGetLastError();
     return -fail(FLETCHER_ERR_NOMEM, "device allocation for shot %zu failed", B.shots.size());
   }
+  HostPins pin;
+  pin.add(model, 6 * s.n * sizeof(float));
   cudaError_t e = cudaMemcpyAsync(raw, model, 6 * s.n * sizeof(float), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(s.coef, 0, s.npitch * kNumCoef * sizeof(float), st);
   if (e == cudaSuccess) {
@@ -1546,6 +1582,8 @@ extern "C" int FLETCHER_BatchGetField(int shot, int which, float *host) {
     k_unpack<<<grid_for(s.n), 256, 0, g_stream>>>(s.F[buf], B.scratch, which & 1, s.sx, s.sy, s.sz, s.pitch);
     CK(cudaGetLastError());
   }
+  HostPins pin;
+  pin.add(host, s.n * sizeof(float), true);
   CK(cudaMemcpyAsync(host, B.scratch, s.n * sizeof(float), cudaMemcpyDeviceToHost, g_stream));
   CK(cudaStreamSynchronize(g_stream));
   // The previous-field buffer lacks the last step's source at the source
