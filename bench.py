@@ -365,7 +365,7 @@ def run_batch_form(args, ws, rank, local, group):
         "metric": "MSamples/s, batched shots (C3)", "value": round(value, 1), "unit": UNIT, "n_gpus": ws,
         "steps": max(p.steps for p in spec), "ms_total": round(ms_max, 1), "higher_is_better": True,
         "scaling": "weak", "dtype": "f32" if form == "fp32" else f"f32 arithmetic, {form} storage",
-        "data": "synthetic (48 seeded layered TTI shots)",
+        "data": f"synthetic ({len(spec)} seeded layered TTI shots)",
         "config": {"workload": f"C3: {len(spec)} shots, n ~ U{{96..320}}/8*8 per axis, 500-1500 steps, dt 0.6 ms, "
                                "one persistent launch per step, CUDA-graph time loop",
                    "storage": form,
