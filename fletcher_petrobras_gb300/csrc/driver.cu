@@ -667,12 +667,13 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
     for (int k = 0; k < 6; ++k) r6.a[k] = src6[k];
   } else {
     CK(cudaMalloc(&raw, 6 * g.n * sizeof(float)));
-    for (int k = 0; k < 6; ++k) pins.add(src6[k], g.n * sizeof(float));
-    for (const float *f : {pp, pc, qp, qc}) pins.add(f, g.n * sizeof(float));
+    // Each array is locked while the copies before it run.
     for (int k = 0; k < 6; ++k) {
+      pins.add(src6[k], g.n * sizeof(float));
       CK(cudaMemcpyAsync(raw + k * g.n, src6[k], g.n * sizeof(float), cudaMemcpyHostToDevice, s));
       r6.a[k] = raw + k * g.n;
     }
+    for (const float *f : {pp, pc, qp, qc}) pins.add(f, g.n * sizeof(float));
   }
   k_precompute<<<grid_for(g.n), 256, 0, s>>>(r6, g.coef, sx, sy, sz, g.pitch);
   CK(cudaGetLastError());
