@@ -10,6 +10,7 @@ the reference's RandomVelocityBoundary applied inside the reference build.
     python tests/golden/make_golden.py --c1       # + the 504^3, 1000-step case (about an hour)
     python tests/golden/make_golden.py --c2-f64   # FP64 oracle, 128^3 interior, 2000 steps (minutes)
     python tests/golden/make_golden.py --d1d1     # the der1der1/ tree (Der1-Der1 formulation), small cases
+    python tests/golden/make_golden.py --aniso    # only the small case with dx != dy != dz
 
 Each fixture stores the problem definition, hashes of the boundary-modified
 velocities and of the reference's coefficient fields, and the final current
@@ -178,13 +179,23 @@ def run_c2_f64(stride: int = 4) -> None:
     print(f"wrote {out} ({os.path.getsize(out) / 1e3:.0f} kB)")
 
 
+# Three different grid spacings (every derivative scaled on its own).
+ANISO = Problem("tiny_aniso", 24, 20, 16, absorb=6, dx=10.0, dy=12.5, dz=15.0, dt=0.0005, steps=60, fcut=45.0,
+                kind="layered", layers=4, seed=5)
+ANISO = ANISO.with_(source=(ANISO.sx // 2 - 2, ANISO.sy // 2 + 1, ANISO.bord + ANISO.absorb + 5))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--c1", action="store_true", help="also run the 504^3 x 1000-step case")
     ap.add_argument("--only-c1", action="store_true")
     ap.add_argument("--c2-f64", action="store_true", help="only the FP64 oracle's 128^3, 2000-step case")
     ap.add_argument("--d1d1", action="store_true", help="only the Der1-Der1 tree's small cases")
+    ap.add_argument("--aniso", action="store_true", help="only the small case with three different spacings")
     a = ap.parse_args()
+    if a.aniso:
+        run_small(ref_lib(), "tiny_aniso", ANISO)
+        return
     if a.c2_f64:
         run_c2_f64()
         return

@@ -73,6 +73,24 @@ def test_short_run_vs_fp64_oracle(form, orc):
     assert not v[:b].any() and not v[-b:].any() and not v[:, :b].any() and not v[:, :, -b:].any()
 
 
+ANISO = Problem("half_aniso", 40, 36, 32, absorb=6, dx=10.0, dy=12.5, dz=15.0, dt=0.0005, steps=150, fcut=45.0,
+                kind="layered", layers=4, seed=13)
+
+
+@pytest.mark.parametrize("form", ["fp16x", "fp16"])
+def test_anisotropic_spacing_vs_fp64_oracle(form, orc):
+    """dx, dy, dz all different: every derivative carries its own inverse
+    spacing (the kernels' non-isotropic path); same bounds as the short run."""
+    m = ANISO.model()
+    (p, q, _, _), _ = run(ANISO, m, form)
+    op, oq = orc.run_f64(ANISO, m)
+    ep, eq = rel_l2(p, op), rel_l2(q, oq)
+    print(f"{form} anisotropic: rel L2 vs FP64 p {ep:.3g} q {eq:.3g}")
+    assert ep < TOL[form]["short"] and eq < TOL[form]["short"]
+    (p32, _, _, _), _ = run(ANISO, m, "fp32")
+    assert rel_l2(p32, op) < 1e-5
+
+
 @pytest.mark.parametrize("form", ["fp16x", "fp16"])
 def test_c2_error_vs_fp64_oracle(form):
     """128^3 interior (200^3 grid), 2000 steps, vs the FP64 oracle fixture."""

@@ -81,7 +81,7 @@ def test_coefficients_match_oracle(orc):
     assert np.count_nonzero(ulp) <= 1e-4 * ulp.size
 
 
-@pytest.mark.parametrize("name", ["tiny_homog", "tiny_layered", "tiny_maintti"])
+@pytest.mark.parametrize("name", ["tiny_homog", "tiny_layered", "tiny_maintti", "tiny_aniso"])
 def test_small_cases_vs_reference(name, orc):
     prob, meta, g = load_golden(name)
     if name == "tiny_maintti":

@@ -7,7 +7,7 @@ import pytest
 
 from conftest import GOLDEN, load_golden, plane_sums, subsample
 
-SMALL = ["tiny_homog", "tiny_layered", "tiny_maintti"]
+SMALL = ["tiny_homog", "tiny_layered", "tiny_maintti", "tiny_aniso"]  # tiny_aniso: dx, dy, dz all differ
 
 
 def sha(a):
