@@ -109,9 +109,12 @@ def test_half_batch_matches_single_shot_runs(form):
 
 
 @pytest.mark.parametrize("form", ["fp32", "fp16x"])
-def test_batch_with_three_spacings_matches_single_shot_runs(form):
-    """dx, dy, dz all different (the kernels' non-isotropic path): batched
-    shots stay bit-identical to their single-shot runs."""
+def test_batch_with_three_spacings_matches_single_shot_runs(form, orc):
+    """dx, dy, dz all different (the kernels' non-isotropic path).  There the
+    last bits of a cell depend on how its tile column is split in z (whole
+    columns, as the batch runs them, or the single-shot plan's segments), so
+    batched shots are compared with their single-shot runs to 1e-6 and with
+    the oracle to 1e-5 rather than bit for bit."""
     sp = dict(dx=10.0, dy=12.5, dz=15.0, dt=0.0005)
     shots = [s.with_(**sp) for s in SHOTS[:2]]
     models = [p.model() for p in shots]
@@ -124,4 +127,7 @@ def test_batch_with_three_spacings_matches_single_shot_runs(form):
     for i, (p, m) in enumerate(zip(shots, models)):
         ref = single(p, m, form)
         for k in range(4):
-            assert np.array_equal(got[i][k], ref[k]), (form, i, k)
+            assert rel_l2(got[i][k], ref[k]) < 1e-6, (form, i, k)
+        op, oq, _, _ = orc.run_f32(p, m)
+        tol = 1e-5 if form == "fp32" else 1e-4
+        assert rel_l2(got[i][0], op) < tol and rel_l2(got[i][1], oq) < tol
