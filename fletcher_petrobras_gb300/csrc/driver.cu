@@ -532,7 +532,10 @@ int setup_tiles(int rows, int stages) {
   g.stages = stages;
   g.ntx = (sx - bord - kRadius + kTileX - 1) / kTileX;
   g.nty = (sy - bord - kRadius + TY - 1) / TY;
-  const int ctas = g.num_sms * propagate_fp32_ctas_per_sm(TY);
+  const int per_sm = half_form() ? propagate_half_ctas_per_sm(TY, stages, g.form == FLETCHER_FORM_FP16X, false)
+                                  : propagate_fp32_ctas_per_sm(TY);
+  if (per_sm < 1) return fail(FLETCHER_ERR_CUDA, "tile shape (%d rows, %d stages) fits no CTA on an SM", TY, stages);
+  const int ctas = g.num_sms * per_sm;
   const Split sp = plan_segments(ctas, g.ntx, g.nty, TY, bord, sz - 2 * bord, g.zchunks);
   if (g.seg) cudaFree(g.seg);
   if (g.cta_first) cudaFree(g.cta_first);
@@ -1210,6 +1213,7 @@ struct Batch {
   float *scratch = nullptr;
   size_t max_n = 0;
   int rows = 12, stages = 5;
+  int ctas = 0;  // persistent CTAs of a launch (resident ones, for the sealed shape)
   long launches = 0;
   size_t dev_bytes = 0;
   int num_sms = 0;
@@ -1358,7 +1362,7 @@ int batch_issue(int it0, int it1, const float *src) {
   P.iso = (B.dx == B.dy && B.dx == B.dz) ? 1 : 0;
   P.dt2 = P.iso ? (B.dt * B.dt) * P.inv_dxx : B.dt * B.dt;
   P.err = B.err_dev;
-  const int ctas = B.num_sms * propagate_fp32_ctas_per_sm(B.sealed_rows);
+  const int ctas = B.ctas;
   int active = ns;  // shots still running, a prefix of B.order
   for (int it = it0; it < it1; ++it) {
     while (active > 0 && B.shots[B.order[active - 1]].nsteps <= it) --active;
@@ -1533,6 +1537,12 @@ extern "C" int FLETCHER_BatchRun(const float *src, int max_steps, int use_graph,
                             ? propagate_half_prepare(B.sealed_rows, B.stages, B.form == FLETCHER_FORM_FP16X, true)
                             : propagate_fp32_prepare(B.sealed_rows, B.stages);
   if (pe != cudaSuccess) return fail(FLETCHER_ERR_CUDA, "kernel attribute set-up failed");
+  const int per_sm = batch_half() ? propagate_half_ctas_per_sm(B.sealed_rows, B.stages,
+                                                               B.form == FLETCHER_FORM_FP16X, true)
+                                  : propagate_fp32_ctas_per_sm(B.sealed_rows);
+  if (per_sm < 1)
+    return fail(FLETCHER_ERR_CUDA, "tile shape (%d rows, %d stages) fits no CTA on an SM", B.sealed_rows, B.stages);
+  B.ctas = B.num_sms * per_sm;
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));

@@ -132,6 +132,7 @@ struct HalfLaunch {
 bool propagate_half_supported(int tile_rows, int stages);
 cudaError_t propagate_half_launch(const HalfLaunch &L, bool ext, cudaStream_t s);
 cudaError_t propagate_half_prepare(int tile_rows, int stages, bool ext, bool batch);
+int propagate_half_ctas_per_sm(int tile_rows, int stages, bool ext, bool batch);
 cudaError_t half_scales(const unsigned *m_cur, unsigned *m_prev, int *e_new, int sz, int src_z, float src_abs,
                         cudaStream_t s);
 // Before a batched 16-bit step: the new field's plane exponents and the
