@@ -131,3 +131,27 @@ def test_batch_with_three_spacings_matches_single_shot_runs(form, orc):
         op, oq, _, _ = orc.run_f32(p, m)
         tol = 1e-5 if form == "fp32" else 1e-4
         assert rel_l2(got[i][0], op) < tol and rel_l2(got[i][1], oq) < tol
+
+
+@pytest.mark.parametrize("form", ["fp32", "fp16", "fp16x"])
+def test_deep_shots_split_in_z_match_single_shot_runs(form):
+    """Shots deeper than one 128-plane chunk: each tile column is several
+    batch items, and the shot's fields still equal its single-shot run."""
+    shots = [
+        Problem("deep0", 40, 30, 150, absorb=4, dt=0.0006, steps=16, fcut=45.0, kind="layered", layers=4, seed=31,
+                source=(20, 15, 60)),
+        Problem("deep1", 33, 20, 262, absorb=3, dt=0.0006, steps=11, fcut=45.0, kind="layered", layers=5, seed=32,
+                source=(18, 12, 140)),
+    ]
+    models = [p.model() for p in shots]
+    batch = Batch(form=form)
+    for p, m in zip(shots, models):
+        batch.add(p, m)
+    batch.run()
+    got = [[batch.field(i, k) for k in range(4)] for i in range(len(shots))]
+    batch.close()
+    for i, (p, m) in enumerate(zip(shots, models)):
+        ref = single(p, m, form)
+        assert np.abs(ref[0]).max() > 0.0
+        for k in range(4):
+            assert np.array_equal(got[i][k], ref[k]), (form, i, k)
