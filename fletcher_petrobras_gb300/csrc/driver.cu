@@ -1171,9 +1171,11 @@ extern "C" int FLETCHER_GetTileConfig(int *rows, int *stages) {
 //
 // Many independent shots of different sizes advance together: one persistent
 // launch per time step covers the work items of every shot that is still
-// running, and the whole time loop is captured in a CUDA graph.  Shots are
-// ordered by step count (longest first), so the shots still running at any
-// step are a prefix of that order and so are their work items.
+// running (16-bit forms: preceded by one launch that sets the new planes'
+// scales of every running shot), and the whole time loop is captured in a
+// CUDA graph.  Shots are ordered by step count (longest first), so the shots
+// still running at any step are a prefix of that order and so are their work
+// items.
 
 #include <algorithm>
 #include <vector>
