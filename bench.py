@@ -212,6 +212,32 @@ def timed_run(prob, model, form, K, W, group, clocks=None):
     return ms, launches, bpc, dev_gb, clk
 
 
+def reference_parity(prob, steps, form, p, q):
+    """Relative L2 of an FP32 run's final p and q against the reference's own
+    OpenMP build on the same problem and step count: the committed fixture
+    tests/golden/golden_c1.npz (504^3 interior, 1000 steps, every 12th cell
+    per axis).  None for any other run."""
+    path = os.path.join(ROOT, "tests", "golden", "golden_c1.npz")
+    if form != "fp32" or not os.path.exists(path):
+        return None
+    g = np.load(path)
+    meta = json.loads(str(g["meta"]))
+    if meta["name"] != prob.name or meta["steps"] != steps or meta["seed"] != prob.seed:
+        return None
+    st = meta["stride"]
+
+    def sub(a):
+        return np.asarray(a).reshape(prob.sz, prob.sy, prob.sx)[::st, ::st, ::st].ravel().astype(np.float64)
+
+    def rel(a, b):
+        b = b.astype(np.float64)
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    return {"vs": f"reference OpenMP build, {steps} steps (tests/golden/golden_c1.npz, every {st}th cell)",
+            "rel_l2_p": float(f"{rel(sub(p), g['p']):.3e}"), "rel_l2_q": float(f"{rel(sub(q), g['q']):.3e}"),
+            "tolerance": 1e-4}
+
+
 def run_gb300(args, ws, rank, local, group):
     import torch
 
@@ -253,7 +279,7 @@ def run_gb300(args, ws, rank, local, group):
     import ctypes as C
 
     stats = (C.c_double * 5)()
-    e2e = e2e_wall = None
+    e2e = e2e_wall = parity = None
     if not args.no_e2e:
         f = np.zeros((4, prob.n), np.float32)
         from fletcher_petrobras_gb300.driver import FORMS
@@ -270,6 +296,7 @@ def run_gb300(args, ws, rank, local, group):
         lib.FLETCHER_ModelPhases(phases)
         e2e_wall = group.reduce(stats[2], "max")
         e2e = ws * cells * K / e2e_wall / 1e6
+        parity = reference_parity(prob, K, form, f[1], f[3])  # FLETCHER_Model leaves the final p, q in pc, qc
         del f
 
     cpu = None
@@ -311,6 +338,8 @@ def run_gb300(args, ws, rank, local, group):
         "gpu_launches": launches,
         "clocks": clk,
     }
+    if parity:
+        line["parity"] = parity
     if forms:
         line["forms"] = forms
     if cpu:
