@@ -10,7 +10,7 @@ the reference's RandomVelocityBoundary applied inside the reference build.
     python tests/golden/make_golden.py --c1       # + the 504^3, 1000-step case (about an hour)
     python tests/golden/make_golden.py --c2-f64   # FP64 oracle, 128^3 interior, 2000 steps (minutes)
     python tests/golden/make_golden.py --d1d1     # the der1der1/ tree (Der1-Der1 formulation), small cases
-    python tests/golden/make_golden.py --aniso    # only the small case with dx != dy != dz
+    python tests/golden/make_golden.py --aniso    # only the small cases with dx != dy != dz (both trees)
 
 Each fixture stores the problem definition, hashes of the boundary-modified
 velocities and of the reference's coefficient fields, and the final current
@@ -195,6 +195,7 @@ def main() -> None:
     a = ap.parse_args()
     if a.aniso:
         run_small(ref_lib(), "tiny_aniso", ANISO)
+        run_small(ref_lib("der1der1"), "d1d1_tiny_aniso", ANISO.with_(name="d1d1_aniso"))
         return
     if a.c2_f64:
         run_c2_f64()

@@ -80,7 +80,7 @@ def test_fp64_oracle_close_to_fp32(orc):
     assert orc.rel_l2(g["q"], q64) < 1e-5
 
 
-@pytest.mark.parametrize("name", ["d1d1_tiny_layered", "d1d1_c0"])
+@pytest.mark.parametrize("name", ["d1d1_tiny_layered", "d1d1_c0", "d1d1_tiny_aniso"])
 def test_der1der1_restatement_bit_identical(name, orc):
     """The Der1-Der1 restatement (orc_propagate_d1d1_f32) against the
     der1der1/ tree's own OpenMP build: identical floats."""
