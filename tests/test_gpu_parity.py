@@ -267,7 +267,7 @@ def test_c1_full_size_vs_reference():
     assert ep < TOL_C1 and eq < TOL_C1 and es < TOL_C1
 
 
-@pytest.mark.parametrize("name", ["d1d1_tiny_layered", "d1d1_c0"])
+@pytest.mark.parametrize("name", ["d1d1_tiny_layered", "d1d1_c0", "d1d1_tiny_aniso"])
 def test_vs_der1der1_reference(name, orc):
     """The GPU path against the der1der1/ tree's output (the Der1-Der1
     formulation): the same 1e-5 bound as against original/.  The GPU's
