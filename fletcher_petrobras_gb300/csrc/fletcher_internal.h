@@ -32,8 +32,9 @@ struct ShotDesc {
   int pad[2];
 };
 
-// TMA descriptors of one shot (64-byte aligned in device memory).
-struct alignas(64) ShotMaps {
+// TMA descriptors of one shot (in device memory; CUtensorMap carries the
+// alignment TMA needs).
+struct ShotMaps {
   CUtensorMap halo[2];  // field buffer b, box (TX+8, TY+8, 1)
   CUtensorMap pt[2];    // field buffer b, box (TX, TY, 1)
   CUtensorMap arr;      // coefficients, box (TX, TY, 3, 1)
