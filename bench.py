@@ -10,22 +10,26 @@ at (288, 288, 44)), synthetic and seeded.  The line printed by rank 0:
             updated cells x steps / time), K steps timed with CUDA events on the
             library's stream, inputs resident in HBM (11+ GB, larger than L2,
             so no flush is needed between steps);
-  e2e       the same metric through the C ABI with host buffers: the
-            reference's Model() sequence (FLETCHER_Model: DRIVER_Initialize with
-            the host-to-device copy of the model and fields, per step
-            InsertSource + Propagate, a device-to-host snapshot of p every
-            0.01 s of simulated time, final read-back), wall-clock;
+  e2e       the same metric through the C ABI with host buffers over the
+            workload's own 1000 steps: the reference's Model() sequence
+            (FLETCHER_Model: DRIVER_Initialize with the host-to-device copy of
+            the model and fields, per step InsertSource + Propagate, a
+            device-to-host snapshot of p every 0.01 s of simulated time, final
+            read-back), wall-clock; `parity` compares its final fields with the
+            reference build's own 1000-step result;
   roofline  the propagate kernel against the measured HBM copy bandwidth;
             algorithmic bytes = 64 B per updated cell (fields 16 B read + 8 B
             written, ten coefficients 40 B);
-  cpu_baseline  the oracle (the reference's FP32 OpenMP loop restated) on
-            this machine's host cores, on a bounded sample (a 16-plane slab).
+  forms     the 16-bit storage forms on the same workload;
+  c3_batch, c4_learned  the batched-shot and learned-boundary workloads;
+  cpu_baseline  the reference's own OpenMP build (oracle/_ref/ref_cli, the
+            unmodified original/ sources compiled on this host) on all host
+            cores, a few full-grid steps timed by its own wtime() region.
 
 N > 1: replicas only -- every rank runs the whole workload on its own GPU,
 no data exchange; timing is the max over ranks, value the sum of cells/time.
-`--impl reference` times the reference's CPU algorithm (the oracle port) on
-the host cores: each step is one propagation of a 16-plane slab of the same
-grid (a bounded sample of the workload).
+`--impl reference` runs the reference's own OpenMP build on the full grid
+(K steps, at most 40) without loading this project's library.
 """
 from __future__ import annotations
 
@@ -238,6 +242,26 @@ def reference_parity(prob, steps, form, p, q):
             "tolerance": 1e-4}
 
 
+def cpu_baseline_leg(prob, model, args):
+    """The reference's own OpenMP build on this host's cores, on a bounded
+    sample of the workload (a few full-grid steps); the oracle port on a
+    slab when that build is absent."""
+    r = reference_cpu(prob, args.cpu_steps, 1)
+    if r is not None:
+        out = {"value": round(r["msamples"], 2), "unit": UNIT, "cores": r["threads"], "kind": "reference",
+               "sample": f"{args.cpu_steps} timed steps (after 1 untimed) of the full {prob.sx}^3 grid, "
+                         f"{r['timed_s']:.1f} s in the reference's wtime() region; the reference's Model() loop "
+                         "over its OpenMP back-end (oracle/_ref/ref_cli)", "build": r["build"]}
+        return out
+    import oracle
+
+    t = oracle.time_slab(prob, model, nplanes=16, min_seconds=args.cpu_seconds)
+    return {"value": round(t["msamples"], 2), "unit": UNIT, "cores": t["threads"], "kind": "port",
+            "sample": f"{t['steps']} FP32 steps of a {t['planes']}-plane slab of the 576^3 grid "
+                      f"({t['cells']} updated cells/step, {t['seconds']:.1f} s), oracle restatement of "
+                      "original/OpenMP/openmp_propagate.c + original/sample.h (reference build absent)"}
+
+
 def run_gb300(args, ws, rank, local, group):
     import torch
 
@@ -280,13 +304,14 @@ def run_gb300(args, ws, rank, local, group):
 
     stats = (C.c_double * 5)()
     e2e = e2e_wall = parity = None
+    KE = args.e2e_steps or prob.steps  # the workload's own step count (1000 at C1)
     if not args.no_e2e:
         f = np.zeros((4, prob.n), np.float32)
         from fletcher_petrobras_gb300.driver import FORMS
 
         lib.FLETCHER_SetForm(FORMS[form])
         group.barrier()
-        rc = lib.FLETCHER_Model(K, prob.i_source, prob.fcut, 0.01, prob.sx, prob.sy, prob.sz, prob.bord, prob.dx,
+        rc = lib.FLETCHER_Model(KE, prob.i_source, prob.fcut, 0.01, prob.sx, prob.sy, prob.sz, prob.bord, prob.dx,
                                 prob.dy, prob.dz, prob.dt, *[fptr(f[k]) for k in range(4)],
                                 *[fptr(model[k]) for k in range(6)], stats)
         if rc:
@@ -295,19 +320,23 @@ def run_gb300(args, ws, rank, local, group):
         phases = (C.c_double * 4)()
         lib.FLETCHER_ModelPhases(phases)
         e2e_wall = group.reduce(stats[2], "max")
-        e2e = ws * cells * K / e2e_wall / 1e6
-        parity = reference_parity(prob, K, form, f[1], f[3])  # FLETCHER_Model leaves the final p, q in pc, qc
+        e2e = ws * cells * KE / e2e_wall / 1e6
+        parity = reference_parity(prob, KE, form, f[1], f[3])  # FLETCHER_Model leaves the final p, q in pc, qc
         del f
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        import oracle
+        cpu = cpu_baseline_leg(prob, model, args)
 
-        r = oracle.time_slab(prob, model, nplanes=16, min_seconds=args.cpu_seconds)
-        cpu = {"value": round(r["msamples"], 2), "unit": UNIT, "cores": r["threads"], "kind": "port",
-               "sample": f"{r['steps']} FP32 steps of a {r['planes']}-plane slab of the 576^3 grid "
-                         f"({r['cells']} updated cells/step, {r['seconds']:.1f} s), oracle restatement of "
-                         "original/OpenMP/openmp_propagate.c + original/sample.h, gcc -O3 -fopenmp"}
+    # C3 (batched shots) and C4 (learned layer) on their own workloads.
+    extra = {}
+    if not args.no_c3c4 and prob.nx == 504:
+        for key, fn in (("c3_batch", lambda: run_batch_form(args, ws, rank, local, group)),
+                        ("c4_learned", lambda: run_learned_form(args, ws, rank, local, group))):
+            try:
+                extra[key] = fn()
+            except Exception as exc:  # reported, not fatal to the C1 line
+                extra[key] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
     group.barrier()
     if rank != 0:
         return
@@ -328,13 +357,13 @@ def run_gb300(args, ws, rank, local, group):
                      "traffic_unit": "GB per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
                      "kernel": KERNEL[form]},
         "e2e": None if e2e is None else {
-                "value": round(e2e, 1), "unit": UNIT, "h2d_bytes_per_step": int(stats[3] / K),
-                "d2h_bytes_per_step": int(stats[4] / K), "wall_s": round(e2e_wall, 3),
+                "value": round(e2e, 1), "unit": UNIT, "h2d_bytes_per_step": int(stats[3] / KE),
+                "d2h_bytes_per_step": int(stats[4] / KE), "wall_s": round(e2e_wall, 3), "steps": KE,
                 "phases_s": {"setup": round(phases[0], 3), "steps": round(phases[1], 3),
                              "snapshot_drain": round(phases[2], 3), "readback_finalize": round(phases[3], 3)},
-                "what": "FLETCHER_Model via the C ABI: DRIVER_Initialize (H2D of 6 model + 4 field arrays, "
-                        "FP64 coefficient precompute) + K x (InsertSource, Propagate) + D2H snapshot of p every "
-                        "0.01 s simulated + final D2H of p,q"},
+                "what": f"FLETCHER_Model via the C ABI, the workload's {KE} steps: DRIVER_Initialize (H2D of 6 "
+                        "model + 4 field arrays, FP64 coefficient precompute) + per step (InsertSource, Propagate) "
+                        "+ D2H snapshot of p every 0.01 s simulated + final D2H of p,q"},
         "gpu_launches": launches,
         "clocks": clk,
     }
@@ -344,10 +373,13 @@ def run_gb300(args, ws, rank, local, group):
         line["forms"] = forms
     if cpu:
         line["cpu_baseline"] = cpu
+    for k, v in extra.items():
+        if v is not None:
+            line[k] = v
     print(json.dumps(line), flush=True)
 
 
-def run_batch_form(args, ws, rank, local, group):
+def run_batch_form(args, ws, rank, local, group, shots=None):
     """C3: 48 independent shots of uneven size in one persistent launch per
     step, the time loop as a CUDA graph, tile shape from the autotuner;
     against the same shots run one after another through the single-shot
@@ -359,7 +391,7 @@ def run_batch_form(args, ws, rank, local, group):
     from fletcher_petrobras_gb300.batch import Batch, multishot_spec
 
     torch.cuda.set_device(local)
-    spec = multishot_spec(args.shots, seed=args.seed + rank)
+    spec = multishot_spec(shots or args.shots, seed=args.seed + rank)
     form = args.batch_form
     t0 = time.time()
     batch = Batch(form=form)
@@ -406,7 +438,7 @@ def run_batch_form(args, ws, rank, local, group):
         line["sequential_single_shot"] = {"ms_total": round(seq_ms, 1),
                                           "value": round(info["cell_steps"] / (seq_ms / 1e3) / 1e6, 1),
                                           "speedup_of_batch": round(seq_ms / ms, 3)}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_learned_form(args, ws, rank, local, group):
@@ -475,34 +507,82 @@ def run_learned_form(args, ws, rank, local, group):
         "reflected_energy_learned_every_step": fin(res["learned"]["reflected_energy"]),
         "forms": forms,
     }
-    print(json.dumps(line), flush=True)
+    return line
+
+
+# Full-grid reference steps per run: the reference's OpenMP path takes about a
+# second per 576^3 step on the GPU host's cores, so a run is capped to end
+# within a few minutes.
+REF_MAX_STEPS = 40
+REF_MAX_WARMUP = 5
+
+
+def reference_cpu(prob, steps, warmup, ftz=False):
+    """The reference's own FP32 OpenMP build (oracle/_ref/ref_cli, the
+    unmodified original/ sources) on the full grid of `prob`, all host cores,
+    timed by its own wtime() region; None if that build is absent."""
+    import oracle
+
+    if not oracle.reference_cli_available(ftz):
+        return None
+    r = oracle.run_reference_cli(prob, steps + warmup, warmup, ftz=ftz, timeout=900)
+    r["build"] = "gcc -O3 -fopenmp" + (" , linked with -ffast-math (FTZ/DAZ start-up only)" if ftz else
+                                       " (original/Makefile flags, IEEE denormals)")
+    return r
 
 
 def run_reference(args, ws, rank, group):
-    """The reference's CPU algorithm (its FP32 OpenMP loop, restated by the
-    oracle) on the host cores, each step one propagation of a 16-plane slab
-    of the same 576^3 grid."""
+    """`--impl reference`: the reference's own CPU implementation of the path
+    on this host's cores, on the same workload (the C1 grid), through its own
+    code: oracle/_ref/ref_cli runs the unmodified original/ front-end pieces
+    (RandomVelocityBoundary, precomp.h, Source) and OpenMP back-end in the
+    Model() loop, timed by the reference's wtime() region.  Rank 0 only.  The
+    product library is not loaded.  Falls back to the oracle restatement on
+    a 16-plane slab when the reference build is absent."""
     if rank != 0:
         return
     import oracle
-    from fletcher_petrobras_gb300 import C1
+    from fletcher_petrobras_gb300.models import C1
 
     prob = C1
-    model = prob.model()
     K, W = args.steps, args.warmup
-    if W:
-        oracle.time_slab(prob, model, nplanes=16, steps=W)
-    r = oracle.time_slab(prob, model, nplanes=16, steps=K)
-    v = round(r["msamples"], 2)
+    k_run, w_run = min(K, REF_MAX_STEPS), min(W, REF_MAX_WARMUP)
+    r = reference_cpu(prob, k_run, w_run)
+    if r is not None:
+        v = round(r["msamples"], 2)
+        sample = (f"{k_run} timed steps (after {w_run} untimed) of the full {prob.sx}^3 grid"
+                  + (f", capped from the {K} requested" if k_run < K else "")
+                  + f"; set-up {r['setup_s'] + r['run_s'] - r['timed_s']:.1f} s untimed")
+        cpu = {"value": v, "unit": UNIT, "cores": r["threads"], "kind": "reference", "sample": sample,
+               "build": r["build"]}
+        ftz = reference_cpu(prob, min(k_run, 5), min(w_run, 1), ftz=True)
+        if ftz is not None:
+            cpu["ftz"] = {"value": round(ftz["msamples"], 2), "steps": ftz["steps"] - ftz["warmup"],
+                          "build": ftz["build"]}
+        ms = 1e3 * r["timed_s"] / k_run
+        workload = (f"C1: plain FP32 single shot, {prob.nx}^3 interior ({prob.sx}^3 grid), bord 4, absorb 32, "
+                    f"dt 0.6 ms, 8-layer seeded TTI, 15 Hz Ricker at {prob.src_xyz}; the reference's OpenMP "
+                    "back-end in its Model() loop")
+        steps_line = k_run
+    else:
+        model = oracle.model(prob)
+        if W:
+            oracle.time_slab(prob, model, nplanes=16, steps=W)
+        t = oracle.time_slab(prob, model, nplanes=16, steps=K)
+        v = round(t["msamples"], 2)
+        cpu = {"value": v, "unit": UNIT, "cores": t["threads"], "kind": "port",
+               "sample": f"{K} steps of a {t['planes']}-plane slab of the 576^3 grid (reference build absent)"}
+        ms = 1e3 * t["seconds"] / K
+        workload = ("C1: plain FP32 single shot, 504^3 interior (576^3 grid); each step is one propagation of a "
+                    f"{t['planes']}-plane slab ({t['cells']} cells)")
+        steps_line = K
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
-        "ms_per_step": round(1e3 * r["seconds"] / K, 3), "higher_is_better": True, "scaling": "weak",
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": steps_line,
+        "warmup": w_run if r is not None else W, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded 8-layer TTI model)",
-        "config": {"workload": "C1: plain FP32 single shot, 504^3 interior (576^3 grid); each step is one "
-                               f"propagation of a {r['planes']}-plane slab ({r['cells']} cells)",
-                   "grid": [prob.sx, prob.sy, prob.sz]},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": r["threads"], "kind": "port",
-                         "sample": f"{K} steps of a {r['planes']}-plane slab of the 576^3 grid"},
+        "config": {"workload": workload, "grid": [prob.sx, prob.sy, prob.sz],
+                   "updated_cells_per_step": prob.updated_cells},
+        "cpu_baseline": cpu,
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -511,10 +591,13 @@ def run_reference(args, ws, rank, group):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="slab sample length when the reference build is absent")
+    ap.add_argument("--cpu-steps", type=int, default=3, help="full-grid steps of the reference build's CPU baseline")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end run (0: the workload's own)")
+    ap.add_argument("--no-c3c4", action="store_true", help="skip the batched-shot and learned-layer sub-benchmarks")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--interior", type=int, default=504, help="interior size n (n^3); 504 is the workload")
@@ -538,10 +621,11 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, ws, rank, group)
-        elif args.form == "batch":
-            run_batch_form(args, ws, rank, local, group)
-        elif args.form == "learned":
-            run_learned_form(args, ws, rank, local, group)
+        elif args.form in ("batch", "learned"):
+            fn = run_batch_form if args.form == "batch" else run_learned_form
+            line = fn(args, ws, rank, local, group)
+            if line is not None:
+                print(json.dumps(line), flush=True)
         else:
             run_gb300(args, ws, rank, local, group)
     finally:

@@ -13,7 +13,13 @@
 // FLETCHER_NOALLOC_MAX_CELLS floats (16 MiB).  Every GPU that loads the
 // library holds it until the process exits.  A grid with more cells than
 // that is rejected.  All calls share the array: two calls whose work
-// overlaps on the GPU (on different streams) race on it.
+// overlaps on the GPU (from concurrent host threads, or on different
+// streams) race on it.
+//
+// Ordering: the unpack runs on FLETCHER_GetStream().  The caller's writes to
+// the pair volume must be ordered before it: issued on that stream (name the
+// caller's stream with FLETCHER_SetStream) or complete before the call.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdio.h>
 
@@ -26,7 +32,42 @@ namespace {
 static __device__ __align__(256) float g_stage[FLETCHER_NOALLOC_MAX_CELLS];
 
 constexpr int kMaxDevices = 64;
-float *g_stage_addr[kMaxDevices] = {nullptr};  // device address of g_stage, per device
+
+// Device address of g_stage, looked up once per device and context: a
+// context that was reset (cudaDeviceReset) reloads the module, so the
+// address is looked up again when the current context's id changes.
+struct StageAddr {
+  unsigned long long ctx_id;
+  float *addr;
+};
+StageAddr g_stage_addr[kMaxDevices] = {};
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+// Unique id of the calling thread's current context (0 if unknown).
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(p);
+    looked_up = true;
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx && get_id(ctx, &id) == CUDA_SUCCESS)
+    return id;
+  return 0;
+}
 
 // One component of a pitched (p, q) pair volume -> `stage` (unpitched).
 __global__ void k_unpack_to_stage(const float2 *__restrict__ pairs, float *__restrict__ stage, int comp, int sx,
@@ -64,15 +105,21 @@ extern "C" int FLETCHER_ReadFieldNoAlloc(const void *dev_pairs, int sx, int sy, 
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return err(FLETCHER_ERR_CUDA, "cudaGetDevice", e);
   if (dev < 0 || dev >= kMaxDevices) return err(FLETCHER_ERR_ARGS, "device ordinal out of range", cudaSuccess);
-  // First call on this device: find the array's device address (host code
-  // cannot use the symbol itself as a device pointer).
-  if (!g_stage_addr[dev]) {
+  // First call on this device (or in a new context of it): find the array's
+  // device address (host code cannot use the symbol itself as a device
+  // pointer).  cudaSetDevice makes the device's primary context current
+  // first (it initialises the context since CUDA 12).
+  e = cudaSetDevice(dev);
+  if (e != cudaSuccess) return err(FLETCHER_ERR_CUDA, "cudaSetDevice", e);
+  const unsigned long long ctx = current_context_id();
+  if (!g_stage_addr[dev].addr || ctx == 0 || g_stage_addr[dev].ctx_id != ctx) {
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_stage);
     if (e != cudaSuccess) return err(FLETCHER_ERR_CUDA, "cudaGetSymbolAddress", e);
-    g_stage_addr[dev] = static_cast<float *>(p);
+    g_stage_addr[dev].addr = static_cast<float *>(p);
+    g_stage_addr[dev].ctx_id = ctx;
   }
-  float *stage = g_stage_addr[dev];
+  float *stage = g_stage_addr[dev].addr;
   cudaStream_t s = static_cast<cudaStream_t>(FLETCHER_GetStream());
   const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
   k_unpack_to_stage<<<grid, 256, 0, s>>>(static_cast<const float2 *>(dev_pairs), stage, comp, sx, sy, sz, pitch);

@@ -253,16 +253,21 @@ void FLETCHER_BatchDestroy(void);
  * wavefield and coefficient volumes up front, or whose time loop must not
  * call cudaMalloc (an allocation there fails once memory is fully reserved,
  * or stalls the stream).  Copies component `comp` (0 = p, 1 = q) of a
- * caller-owned (p, q) pair volume on the current device -- float pairs,
- * [sz][sy][pitch], x fastest, pitch >= sx, the layout of this library's own
- * field buffers -- into host_out (sx*sy*sz floats).  It allocates nothing:
- * it stages through a fixed array of FLETCHER_NOALLOC_MAX_CELLS floats
- * (16 MiB) built into the library, which every GPU that loads the library
- * holds until the process exits; larger grids are rejected with
- * FLETCHER_ERR_ARGS.  The first call on a device looks up that array's
- * device address, so make it before any stream capture.  Calls share the
- * array: calls that overlap on the GPU race.  Runs on FLETCHER_GetStream()
- * and returns when host_out is filled; returns a FLETCHER_* status. */
+ * caller-owned (p, q) pair volume on the current device -- float2 pairs,
+ * [sz][sy][pitch], x fastest, pitch (in pairs) >= sx: the layout of the FP32
+ * form's field buffers (the 16-bit forms store half2 and are not accepted)
+ * -- into host_out (sx*sy*sz floats).  It allocates nothing: it stages
+ * through a fixed array of FLETCHER_NOALLOC_MAX_CELLS floats (16 MiB) built
+ * into the library, which every GPU that loads the library holds until the
+ * process exits; larger grids are rejected with FLETCHER_ERR_ARGS.  The
+ * first call on a device (and the first after that device's context was
+ * reset) looks up that array's device address, so make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * (from concurrent host threads, or on different streams) race on it.  Runs
+ * on FLETCHER_GetStream(): the caller's writes to dev_pairs must be ordered
+ * before the call -- issued on that stream (FLETCHER_SetStream names the
+ * caller's stream) or complete before it.  Returns when host_out is filled;
+ * returns a FLETCHER_* status. */
 #define FLETCHER_NOALLOC_MAX_CELLS (4u * 1024u * 1024u)
 int FLETCHER_ReadFieldNoAlloc(const void *dev_pairs, int sx, int sy, int sz, int pitch, int comp,
                               float *host_out);

@@ -23,8 +23,8 @@ _lib = None
 
 
 def build() -> str:
-    src = os.path.join(HERE, "fletcher_oracle.c")
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("fletcher_oracle.c", "model_layered.c")]
+    if not os.path.exists(LIB) or any(os.path.getmtime(LIB) < os.path.getmtime(s) for s in srcs):
         subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     return LIB
 
@@ -50,6 +50,7 @@ def load():
         lib.orc_threads.restype = C.c_int
         lib.orc_recommended_dt.restype = C.c_float
         lib.orc_recommended_dt.argtypes = [C.c_long, FP, FP, C.c_float, C.c_float, C.c_float]
+        lib.orc_model_layered.argtypes = [C.c_int] * 6 + [C.c_uint64, C.c_float, C.c_float, C.c_float, FP]
         _lib = lib
     return _lib
 
@@ -60,6 +61,23 @@ def _fp(a):
 
 def _dp(a):
     return a.ctypes.data_as(DP)
+
+
+def model_layered(prob) -> np.ndarray:
+    """(6, n) float32 layered medium of a layered `Problem` before the
+    boundary (oracle/model_layered.c; equal to the product's generator)."""
+    lib = load()
+    m = np.empty((6, prob.n), np.float32)
+    lib.orc_model_layered(prob.sx, prob.sy, prob.sz, prob.bord, prob.absorb, prob.layers, prob.seed,
+                          float(prob.vrange[0]), float(prob.vrange[1]), float(prob.vs_ratio), _fp(m))
+    return m
+
+
+def model(prob) -> np.ndarray:
+    """(6, n) float32 model of a layered `Problem` with the random-velocity
+    boundary applied, built by the oracle alone (no product library)."""
+    m = model_layered(prob)
+    return boundary(prob.sx, prob.sy, prob.sz, prob.nx, prob.ny, prob.nz, prob.bord, prob.absorb, m, prob.seed)
 
 
 def boundary(sx, sy, sz, nx, ny, nz, bord, absorb, model: np.ndarray, seed: int) -> np.ndarray:
@@ -184,3 +202,41 @@ def time_slab(prob, model: np.ndarray, nplanes: int = 16, min_seconds: float = 1
     el = time.perf_counter() - t0
     return {"msamples": 1e-6 * cells * n / el, "steps": n, "seconds": el, "cells": cells, "threads": threads(),
             "planes": z1 - z0}
+
+
+REF_CLI = os.path.join(HERE, "_ref", "ref_cli")
+REF_CLI_FTZ = os.path.join(HERE, "_ref", "ref_cli_ftz")
+
+
+def reference_cli_available(ftz: bool = False) -> bool:
+    return os.access(REF_CLI_FTZ if ftz else REF_CLI, os.X_OK)
+
+
+def run_reference_cli(prob, steps: int, warmup: int = 0, ftz: bool = False, threads: int | None = None,
+                      out: str = "-", stride: int = 1, timeout: float | None = None) -> dict:
+    """Runs the reference's own FP32 OpenMP path (oracle/_ref/ref_cli, built
+    from the unmodified original/ sources) on a layered `Problem`, in a
+    separate process: the medium from oracle/model_layered.c, srand(seed) +
+    RandomVelocityBoundary, precompute, then the Model() loop for `steps`
+    steps.  Timing is the reference's own wtime() region (DRIVER_Propagate +
+    SwapArrays, original/model.c:82-88) over the steps after `warmup`.
+    Returns dict(msamples, timed_s, threads, setup_s, run_s, steps, warmup)."""
+    exe = REF_CLI_FTZ if ftz else REF_CLI
+    if not os.access(exe, os.X_OK):
+        raise FileNotFoundError(exe)
+    ix, iy, iz = prob.src_xyz
+    spec = f"layered:{prob.layers}:{prob.vrange[0]}:{prob.vrange[1]}:{prob.vs_ratio}"
+    args = [exe, spec, out, *map(str, [prob.sx, prob.sy, prob.sz, prob.nx, prob.ny, prob.nz, prob.bord, prob.absorb,
+                                       prob.dx, prob.dy, prob.dz, prob.dt, steps, ix, iy, iz, prob.fcut, prob.seed,
+                                       stride, warmup])]
+    env = dict(os.environ)
+    if threads:
+        env["OMP_NUM_THREADS"] = str(threads)
+    r = subprocess.run(args, capture_output=True, text=True, env=env, timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError(f"ref_cli failed ({r.returncode}): {r.stderr.strip()[-400:]}")
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("ref_cli:")][-1].split()
+    kv = dict(zip(line[1::2], line[2::2]))
+    return {"msamples": float(kv["msamples"]), "timed_s": float(kv["timed_s"]), "threads": int(kv["threads"]),
+            "setup_s": float(kv["setup_s"]), "run_s": float(kv["run_s"]), "steps": int(kv["steps"]),
+            "warmup": int(kv["warmup"])}

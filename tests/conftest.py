@@ -50,6 +50,14 @@ def orc():
     return oracle
 
 
+def reference_dir():
+    """The reference checkout's root (holding original/ and der1der1/):
+    $FLETCHER_REF_DIR when set, else the copy staged by `make -C oracle stage`
+    in oracle/_ref/src; None when neither holds original/main.c."""
+    d = os.environ.get("FLETCHER_REF_DIR") or os.path.join(ROOT, "oracle", "_ref", "src")
+    return d if os.path.isfile(os.path.join(d, "original", "main.c")) else None
+
+
 def gpu_available() -> bool:
     try:
         import torch

@@ -6,12 +6,13 @@ compute in FP32.  FP16 keeps an 11-bit significand per value, FP16X a 19-bit
 one (FP16 plus a residual byte).  The error vs the FP64 oracle (relative L2
 of p and q over the compared cells) is bounded per form:
 
-* 128^3 interior, 2000 steps (the 16-bit storage case): FP16X <= 1e-3.
-  FP16 misses that bound: its per-step rounding (2^-12 of each value)
-  accumulates through the leapfrog update (p_next = 2 p - p_prev + ...),
-  whose near-zero-frequency modes integrate the rounding noise, and reaches
-  O(0.5) after 2000 steps; the test records it and only checks that it
-  stays finite and below 1.
+* 128^3 interior, 2000 steps (the 16-bit storage case): <= 1e-3 for both
+  forms.  FP16X meets it.  FP16 does not, and its test is an expected
+  failure (xfail, strict) that names the miss: its per-step rounding (2^-12
+  of each value) accumulates through the leapfrog update
+  (p_next = 2 p - p_prev + ...), whose near-zero-frequency modes integrate
+  the rounding noise, and reaches 0.45 (p) / 0.58 (q) after 2000 steps.  A
+  separate test only checks that FP16 stays finite and below 1 there.
 * short runs (150 steps): FP16X <= 1e-4, FP16 <= 2e-2.
 
 Results that do not depend on the launch shape (tile rows, stages,
@@ -25,7 +26,9 @@ from fletcher_petrobras_gb300 import C2, FletcherError, Problem, Propagator
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp16x": {"short": 1e-4, "c2": 1e-3}, "fp16": {"short": 2e-2, "c2": 1.0}}
+TOL = {"fp16x": {"short": 1e-4, "c2": 1e-3}, "fp16": {"short": 2e-2, "c2": 1e-3}}
+FP16_C2_MISS = ("FP16 storage (11-bit significand) misses the 1e-3 C2 bound: relative L2 0.45 (p) / 0.58 (q) "
+                "after 2000 steps; FP16X is the 16-bit-storage form that meets it")
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -91,9 +94,7 @@ def test_anisotropic_spacing_vs_fp64_oracle(form, orc):
     assert rel_l2(p32, op) < 1e-5
 
 
-@pytest.mark.parametrize("form", ["fp16x", "fp16"])
-def test_c2_error_vs_fp64_oracle(form):
-    """128^3 interior (200^3 grid), 2000 steps, vs the FP64 oracle fixture."""
+def c2_errors(form):
     prob, meta, g = load_golden("c2_f64")
     assert prob == C2
     (p, q, _, _), _ = run(prob, prob.model(), form)
@@ -101,7 +102,23 @@ def test_c2_error_vs_fp64_oracle(form):
     ep, eq = rel_l2(subsample(p, prob, s), g["p"]), rel_l2(subsample(q, prob, s), g["q"])
     es = rel_l2(plane_sums(p, prob), g["psum"])
     print(f"{form} C2: rel L2 vs FP64 p {ep:.3g} q {eq:.3g}; plane energy {es:.3g}")
+    return ep, eq
+
+
+@pytest.mark.parametrize("form", ["fp16x", pytest.param("fp16", marks=pytest.mark.xfail(strict=True,
+                                                                                        reason=FP16_C2_MISS))])
+def test_c2_error_vs_fp64_oracle(form):
+    """128^3 interior (200^3 grid), 2000 steps, vs the FP64 oracle fixture:
+    the 16-bit storage contract, relative L2 <= 1e-3 for p and q."""
+    ep, eq = c2_errors(form)
     assert ep < TOL[form]["c2"] and eq < TOL[form]["c2"]
+
+
+def test_c2_fp16_stays_bounded():
+    """FP16 on the same case: not within the contract (above), but finite
+    and below 1."""
+    ep, eq = c2_errors("fp16")
+    assert np.isfinite(ep) and np.isfinite(eq) and ep < 1.0 and eq < 1.0
 
 
 def test_c2_fp32_form_vs_fp64_oracle():

@@ -10,7 +10,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, ROOT, load_golden
+from conftest import GOLDEN, ROOT, load_golden, reference_dir
 from fletcher_petrobras_gb300 import C0, C1, C2, Problem
 from fletcher_petrobras_gb300._lib import SIGNATURES, fptr
 
@@ -117,11 +117,12 @@ def test_argument_errors_are_reported_not_fatal(lib):
     assert lib.FLETCHER_SetTileConfig(0, 0, 0) == 0
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/original"), reason="reference checkout absent")
+@pytest.mark.skipif(reference_dir() is None, reason="reference sources absent (FLETCHER_REF_DIR or staged copy)")
 def test_reference_front_end_links_against_library(tmp_path):
     """The reference's own front-end objects link against libfletcher_gb300.so
-    in place of a back-end (the drop-in link line of original/Makefile:29-31)."""
-    ref = "/root/reference/original"
+    in place of a back-end (the drop-in link line of original/Makefile:29-31).
+    tests/test_gpu_dropin.py runs the result on a GPU."""
+    ref = os.path.join(reference_dir(), "original")
     objs = []
     for src in ["main.c", "source.c", "utils.c", "boundary.c", "walltime.c", "model.c", "map.c"]:
         o = tmp_path / (src + ".o")
@@ -146,3 +147,37 @@ def test_multishot_spec_properties():
         ix, iy, iz = p.src_xyz
         b = p.bord + p.absorb
         assert b <= iz < b + max(1, p.nz // 4) and b <= ix < b + p.nx and b <= iy < b + p.ny
+
+
+def test_oracle_layered_model_matches_library():
+    """The oracle's layered-medium generator (used by the benchmark's
+    reference arm, which must not load this library) gives the library's
+    floats, before and after the random-velocity boundary."""
+    import oracle
+    from fletcher_petrobras_gb300.models import C2, Problem
+
+    for prob in (Problem("lay", 40, 36, 32, absorb=6, dt=0.0006, kind="layered", layers=4, seed=3),
+                 Problem("lay1", 24, 20, 30, absorb=5, dt=0.0006, kind="layered", layers=1, seed=7),
+                 Problem("lay9", 20, 20, 12, absorb=4, dt=0.0006, kind="layered", layers=9, seed=11), C2):
+        assert np.array_equal(oracle.model_layered(prob), prob.raw_model()), prob.name
+        assert np.array_equal(oracle.model(prob), prob.model()), prob.name
+
+
+@pytest.mark.skipif(reference_dir() is None, reason="reference sources absent (FLETCHER_REF_DIR or staged copy)")
+def test_reference_cli_matches_reference_library():
+    """oracle/_ref/ref_cli (the reference's own OpenMP build driven by the
+    reference arm of the benchmark) reproduces the reference fixture of a
+    layered case bit for bit, and reports its wtime() region."""
+    import tempfile
+
+    import oracle
+
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True, capture_output=True)
+    prob, meta, g = load_golden("tiny_layered")
+    with tempfile.TemporaryDirectory() as d:
+        out = os.path.join(d, "o.bin")
+        r = oracle.run_reference_cli(prob, prob.steps, 2, out=out, threads=2)
+        n = prob.n
+        f = np.fromfile(out, np.float32, count=2 * n)
+    assert r["steps"] == prob.steps and r["warmup"] == 2 and r["timed_s"] > 0 and r["threads"] == 2
+    assert np.array_equal(f[:n], g["p"]) and np.array_equal(f[n:], g["q"])

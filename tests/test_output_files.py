@@ -8,17 +8,16 @@ import os
 import numpy as np
 import pytest
 
-from conftest import ROOT
+from conftest import ROOT, reference_dir
 
-REF_SRC = "/root/reference/original"
 REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libfletcher_ref.so")
 FP = C.POINTER(C.c_float)
 
 
 @pytest.fixture(scope="module")
 def ref():
-    if not os.path.isdir(REF_SRC):
-        pytest.skip("reference checkout not present")
+    if reference_dir() is None:
+        pytest.skip("reference sources absent (FLETCHER_REF_DIR or staged copy)")
     import subprocess
 
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True, capture_output=True)

@@ -2,8 +2,10 @@
 device memory (codes that reserve the whole GPU for their own volumes, or
 whose time loop must not call cudaMalloc).  It must return exactly what the
 regular read-back (FLETCHER_GetField) returns for the same field, call after
-call, while allocating nothing itself.  Kept in its own file so pytest runs
-it after every other test."""
+call, while allocating nothing itself.  The file name makes pytest collect it
+last, so that if it fails, a run that stops at the first failure
+(`pytest -x`) has already run every other test; it passes alone in a fresh
+process as well as after the others."""
 import ctypes as C
 
 import numpy as np
@@ -61,3 +63,35 @@ def test_rejects_grids_beyond_the_staging_array():
     assert rc == 1
     assert b"exceeds" in lib.FLETCHER_GetLastErrorString()
     lib.FLETCHER_ClearError()
+
+
+def test_orders_after_writes_on_the_callers_stream():
+    """The volume is written on the caller's own stream, which is named with
+    FLETCHER_SetStream; the read-back must see the finished writes without a
+    device-wide synchronisation in between."""
+    import torch
+
+    lib = load()
+    sx, sy, sz, pitch = 40, 24, 20, 48
+    n = sx * sy * sz
+    g = np.random.default_rng(11)
+    vals = g.standard_normal((sz, sy, pitch, 2)).astype(np.float32)
+    host = torch.from_numpy(vals).pin_memory()
+    dev = torch.zeros((sz, sy, pitch, 2), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    try:
+        for comp in (0, 1):
+            dev.zero_()
+            torch.cuda.synchronize()
+            with torch.cuda.stream(side):
+                torch.cuda._sleep(20_000_000)  # keeps the stream busy ~10 ms before the write lands
+                dev.copy_(host, non_blocking=True)
+            assert lib.FLETCHER_SetStream(C.c_void_p(side.cuda_stream)) == 0
+            out = np.full(n, np.nan, np.float32)
+            rc = lib.FLETCHER_ReadFieldNoAlloc(C.c_void_p(dev.data_ptr()), sx, sy, sz, pitch, comp, fptr(out))
+            assert rc == 0, lib.FLETCHER_GetLastErrorString()
+            assert np.array_equal(out, vals[:, :, :sx, comp].ravel())
+    finally:
+        lib.FLETCHER_SetStream(None)
+        torch.cuda.synchronize()
