@@ -33,9 +33,12 @@
 //
 // Network: 40 -> 32 -> 32 -> 2, tanh, FP16 weights and FP16 activations
 // between layers, FP32 accumulation and FP32 biases.
-//   * inference (k_abc_infer) runs on the tensor cores (mma.sync m16n8k16,
-//     f16 x f16 -> f32): one warp evaluates 16 ghost cells, the layer-1 and
-//     layer-2 outputs stay in registers as the next layer's A fragments;
+//   * inference runs on the tensor cores (mma.sync m16n8k16, f16 x f16 ->
+//     f32) inside the boundary kernel (k_abc_boundary, one cooperative launch
+//     after the plain step that also applies the one-way update): one warp
+//     evaluates 16 ghost cells, the layer-1 and layer-2 outputs stay in
+//     registers as the next layer's A fragments, and k stays in registers
+//     until the update uses it;
 //   * training (k_abc_train) is a per-sample forward and backward pass in
 //     FP32 with the same roundings (straight-through), block sums of the
 //     gradients added up in block order (k_abc_reduce: training is
@@ -536,101 +539,6 @@ constexpr int kInferWarps = 8;
 
 __device__ __forceinline__ float sigmoid(float y) { return 1.0f / (1.0f + __expf(-y)); }
 
-// One-way coefficients of every ghost cell from the current and previous
-// fields: gather, normalisation and the network in one kernel.  A warp
-// takes 16 consecutive cells, 4 rays (rays start at multiples of 4 cells).
-// The 4 ghost cells of a ray (d = L-3 .. L) read the 8 points d = L-7 .. L
-// of its normal line (points past the layer read as zero): lane 8r + q
-// loads point q of ray r at t and t-1 once into shared memory (the next
-// tile's loads are issued before this tile's network runs); then two lanes
-// per cell, one for each time, build the cell's stencils from it.
-// k[i] = (k_p, k_q).
-constexpr int kInferBlocksPerSm = 2;  // 128 registers a thread (the network stays in registers)
-
-__global__ void __launch_bounds__(32 * kInferWarps, kInferBlocksPerSm) k_abc_infer(
-    const __grid_constant__ Ghost G, const float2 *__restrict__ cur, const float2 *__restrict__ prev, int sy,
-    int pitch, const float4 *__restrict__ med, const NetHalf *__restrict__ net, float2 *__restrict__ kout) {
-  __shared__ __align__(16) __half Xs[kInferWarps][16 * kXs];
-  __shared__ float2 Ln[kInferWarps][2][4][8];  // [time: t, t-1][ray][point] (p, q)
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = lane >> 1, half_t = lane & 1;
-  Frags F;
-  load_frags(net, F);
-  __half *X = Xs[warp];
-  const long ncells = G.off[6];
-  const long ntiles = (ncells + 15) / 16;
-  const long tstep = (long)gridDim.x * kInferWarps;
-  // This lane's line point (ray lane/8, point lane%8) and its cell's medium
-  // for a tile, loaded a tile ahead (addresses from the ray index alone).
-  auto load_tile = [&](long tile, float2 &a, float2 &b, float4 &m) {
-    const int ray = lane >> 3, q = lane & 7;
-    const long i0 = tile * 16 + 4 * ray;  // the ray's cell d = L-3
-    const long ci = tile * 16 + r;
-    a = b = make_float2(0.f, 0.f);
-    m = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (tile < ntiles && i0 < ncells) {
-      int f;
-      const long base = ghost_index(G, i0, sy, pitch, f);  // sets f, which the step below needs
-      const long at = base + (long)(q - kGhostD) * normal_step(f, sy, pitch);
-      a = cur[at];
-      b = prev[at];
-    }
-    if (tile < ntiles && ci < ncells) m = med[ci];
-  };
-  long tile = blockIdx.x * (long)kInferWarps + warp;
-  float2 pa, pb;
-  float4 pm;
-  load_tile(tile, pa, pb, pm);
-  for (; tile < ntiles; tile += tstep) {
-    Ln[warp][0][lane >> 3][lane & 7] = pa;
-    Ln[warp][1][lane >> 3][lane & 7] = pb;
-    const long ci = tile * 16 + r;
-    const float4 m = pm;
-    load_tile(tile + tstep, pa, pb, pm);
-    __syncwarp();
-    float vv[18];
-    float s = 0.f;
-    const int j = r & 3;  // d = L-3 + j: line points j .. j+8 (past 7: zero)
-    const float2 *line = Ln[warp][half_t][r >> 2];
-#pragma unroll
-    for (int o = 0; o < 9; ++o) {
-      const int q = j + o;
-      const float2 u = (q < 8 && ci < ncells) ? line[q < 8 ? q : 7] : make_float2(0.f, 0.f);
-      vv[o] = u.x;
-      vv[9 + o] = u.y;
-    }
-#pragma unroll
-    for (int k = 0; k < 18; ++k) s = fmaxf(s, fabsf(vv[k]));
-    s = fmaxf(s, __shfl_xor_sync(0xffffffffu, s, 1));
-    // Stencils this small carry no wave (the first cells a front reaches
-    // hold values near the FP32 underflow, whose reciprocal overflows).
-    if (!(s > kMinScale)) s = 0.f;
-    const float inv = s > 0.f ? 1.0f / s : 0.f;
-    __half *row = X + r * kXs + 18 * half_t;
-#pragma unroll
-    for (int k = 0; k < 18; k += 2)
-      *reinterpret_cast<__half2 *>(row + k) = __floats2half2_rn(vv[k] * inv, vv[k + 1] * inv);
-    if (half_t == 0) {
-      const int d = G.L - kGhostD + 1 + j;
-      *reinterpret_cast<__half2 *>(X + r * kXs + 36) = __floats2half2_rn(m.x * kVScale, m.y);
-      *reinterpret_cast<__half2 *>(X + r * kXs + 38) = __floats2half2_rn(m.z, (float)d / (float)G.L);
-    } else {
-#pragma unroll
-      for (int k = 40; k < kK1; k += 2) *reinterpret_cast<__half2 *>(X + r * kXs + k) = __floats2half2_rn(0.f, 0.f);
-    }
-    __syncwarp();
-    float ylo[2], yhi[2];
-    mlp16(X, F, ylo, yhi);
-    const int g = lane >> 2;
-    if ((lane & 3) == 0) {
-      const long c0 = tile * 16 + g, c1 = tile * 16 + g + 8;
-      if (c0 < ncells) kout[c0] = make_float2(sigmoid(ylo[0]), sigmoid(ylo[1]));
-      if (c1 < ncells) kout[c1] = make_float2(sigmoid(yhi[0]), sigmoid(yhi[1]));
-    }
-    __syncwarp();
-  }
-}
-
 // The network on given features (rows of 40 floats), raw outputs.
 __global__ void __launch_bounds__(32 * kInferWarps) k_abc_forward(const float *feat, long n, const NetHalf *net,
                                                                    float *out) {
@@ -665,73 +573,216 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_abc_forward(const float *f
   }
 }
 
-// The one-way update of the rays of the two faces normal to axis A, after
-// the plain step: next[g] = cur[i] + k (cur[g] - next[i]) outward from
-// d = L-3.  Four lanes per ray, one per cell (d = L-3 + lane % 4): each
-// loads its cell's coefficient and current value (the inward one comes from
-// the lane before), the lane of d = L-3 also the inward neighbour's current
-// and next values; the outward dependence next_d = A_d - k_d next_(d-1)
-// (A_d = cur_(d-1) + k_d cur_d) is an inclusive scan of affine maps over the
-// 4 lanes (two shuffle rounds).  Grid: x over (first transverse coordinate,
-// lane), y the second transverse coordinate, z the side.  The rays of one
-// face are independent.
-template <int A>
-__global__ void __launch_bounds__(256) k_abc_rays(const __grid_constant__ Ghost G, const float2 *__restrict__ cur,
-                                                  float2 *__restrict__ next, int sy, int pitch,
-                                                  const float2 *__restrict__ k) {
-  constexpr int T0 = A == 0 ? 1 : 0, T1 = A == 2 ? 1 : 2;
-  const int e0 = G.keep.hi[T0] - G.keep.lo[T0];
-  const int lane = threadIdx.x & 31, j = lane & 3;
-  const int u = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 2);
-  const int v = blockIdx.y;
-  const int side = blockIdx.z;  // 0: the low face, 1: the high one
-  const int f = 2 * (2 - A) + side;
-  const bool live = u < e0;
-  const int d = G.L - kGhostD + 1 + j;
-  int c[3];
-  c[T0] = G.keep.lo[T0] + u;
-  c[T1] = G.keep.lo[T1] + v;
-  c[A] = side ? G.in.hi[A] - 1 + d : G.in.lo[A] - d;
-  const int stride = A == 0 ? 1 : (A == 1 ? pitch : sy * pitch);
-  const int step = side ? stride : -stride;
-  const int gidx = (c[2] * sy + c[1]) * pitch + c[0];
-  float2 kk = make_float2(0.f, 0.f), cg = kk, ci = kk, ni = kk;
-  if (live) {
-    kk = k[G.off[f] + ((long)v * e0 + u) * kGhostD + j];
-    cg = cur[gidx];
-    if (j == 0) {
-      ci = cur[gidx - step];
-      ni = next[gidx - step];
+// ---- the boundary step: one cooperative launch after the plain step -----------
+//
+// For the face pairs normal to z, then y, then x (a bounded grid-wide
+// barrier between them: a pass reads the next values the previous pass wrote
+// at edge cells), every warp takes groups of 4 consecutive rays (16 ghost
+// cells):
+//  1. lane 8 r + q loads point q (d = L-7+q) of ray r's outward normal line
+//     at t from the current field and, in the learned form, at t-1 from the
+//     line buffer the previous launch filled; it stores the t line for the
+//     next launch;
+//  2. learned form, on an evaluation step: the 16 cells' features and the
+//     network on the tensor cores (mma.sync m16n8k16), two lanes per cell
+//     building the t and t-1 stencils; k = sigmoid(y) stays in registers
+//     (it is written to the coefficient buffer only when later steps reuse
+//     it); otherwise k comes from that buffer;
+//  3. lanes 4 r + j (j = 0..3: d = L-3+j) apply the box-scheme update
+//     next_g = cur_i + k (cur_g - next_i) outward along ray r, an inclusive
+//     scan of affine maps over the ray's 4 lanes.
+// The line buffer replaces the read of the t-1 field, which the plain step
+// has overwritten by the time this kernel runs.
+struct BoundaryArgs {
+  Ghost G;
+  const float2 *cur;        // field at t
+  float2 *next;             // field at t+1 (the plain step's result)
+  int sy, pitch;
+  const float4 *med;        // per ghost cell: vpz, epsilon, delta, field index (int bits)
+  const NetHalf *net;
+  const float2 *line_in;    // per ray: the 8 line points at t-1 (learned form)
+  float2 *line_out;         // per ray: the 8 line points at t, for the next launch (learned form)
+  float2 *k;                // per ghost cell: (k_p, k_q), read unless the network runs, written when it is kept
+  int eval;                 // the network runs at this step
+  int keep;                 // store the network's k for the steps that reuse it
+  unsigned *bar;            // grid barrier: arrival count, generation
+  unsigned *err;            // error word (bit 0: a bounded wait gave up)
+  unsigned long long wait_ns;
+};
+
+constexpr int kBoundaryWarps = 8;
+
+// Grid-wide barrier of a cooperative launch (every block is resident),
+// bounded: false when the other blocks have not all arrived within limit_ns
+// (bit 0 of the error word is then set).
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks, uint64_t limit_ns, unsigned *err) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *gen = bar + 1;
+    const unsigned g0 = *gen;
+    __threadfence();
+    int ok = 1;
+    if (atomicAdd(bar, 1u) == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      const uint64_t t0 = global_ns();
+      while (*gen == g0) {
+        if (global_ns() - t0 > limit_ns) {
+          ok = 0;
+          atomicOr(err, 1u);
+          break;
+        }
+        __nanosleep(100);
+      }
     }
+    __threadfence();
+    ok_s = ok;
   }
-  // The inward cell of lanes 1 .. 3 is the cell of the lane before.
-  {
-    const float ux = __shfl_up_sync(0xffffffffu, cg.x, 1), uy = __shfl_up_sync(0xffffffffu, cg.y, 1);
-    if (j != 0) ci = make_float2(ux, uy);
-  }
-  // a_d = cur_(d-1) + k_d cur_d, next_d = a_d - k_d next_(d-1): lane j
-  // folds in lanes j-1 .. 0 of its ray (the first one brings next_(L-4)).
-  float ax = __fmaf_rn(kk.x, cg.x, ci.x), ay = __fmaf_rn(kk.y, cg.y, ci.y);
-  float mx = -kk.x, my = -kk.y;  // coefficient of next_(start-1) in the running value
-  if (j == 0) {
-    ax = __fmaf_rn(mx, ni.x, ax);
-    ay = __fmaf_rn(my, ni.y, ay);
-    mx = 0.f;
-    my = 0.f;
-  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+template <bool NET>
+__global__ void __launch_bounds__(32 * kBoundaryWarps, 2) k_abc_boundary(const __grid_constant__ BoundaryArgs B) {
+  __shared__ __align__(16) __half Xs[NET ? kBoundaryWarps : 1][16 * kXs];
+  __shared__ float2 Ln[kBoundaryWarps][NET ? 2 : 1][4][8];  // [time: t, t-1][ray][point] (p, q)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const Ghost &G = B.G;
+  Frags F;
+  if (NET && B.eval) load_frags(B.net, F);
+  const long wg = (long)blockIdx.x * kBoundaryWarps + warp, nw = (long)gridDim.x * kBoundaryWarps;
+  for (int A = 2; A >= 0; --A) {
+    const int fa = 2 * (2 - A);                       // the low face; fa + 1 is the high one
+    const long r0 = G.off[fa] / kGhostD, rmid = G.off[fa + 1] / kGhostD, r1 = G.off[fa + 2] / kGhostD;
+    const long ngroups = (r1 - r0 + 3) / 4;
+    const int stride = A == 0 ? 1 : (A == 1 ? B.pitch : B.sy * B.pitch);
+    for (long grp = wg; grp < ngroups; grp += nw) {
+      const long ray0 = r0 + 4 * grp;
+      // 1. the rays' lines (lane 8 r + q: point q of ray r).
+      {
+        const int r = lane >> 3, q = lane & 7;
+        const long ray = ray0 + r;
+        float2 a = make_float2(0.f, 0.f), b = a;
+        if (ray < r1) {
+          const int idx0 = __float_as_int(B.med[ray * kGhostD].w);  // cell d = L-3 (point 4)
+          const int step = ray < rmid ? -stride : stride;
+          a = __ldcg(B.cur + idx0 + (q - kGhostD) * step);
+          if constexpr (NET) {
+            if (B.eval) b = __ldcg(B.line_in + ray * 8 + q);
+            __stcg(B.line_out + ray * 8 + q, a);
+          }
+        }
+        Ln[warp][0][r][q] = a;
+        if constexpr (NET) Ln[warp][NET ? 1 : 0][r][q] = b;
+      }
+      __syncwarp();
+      // 2. the coefficient of update lane u = 4 r + j (cell 4 r + j of the group).
+      const int u = lane & 15;
+      const long cell = ray0 * kGhostD + u;
+      const bool live = lane < 16 && ray0 + (u >> 2) < r1;
+      float2 kc = make_float2(0.f, 0.f);
+      if (NET && B.eval) {
+        // Features of cell c = lane / 2 (ray c / 4, d = L-3 + c % 4); the
+        // lane pair builds the t (even lane) and t-1 (odd lane) stencils.
+        const int c = lane >> 1, half_t = lane & 1, j = c & 3;
+        const bool clive = ray0 + (c >> 2) < r1;
+        const float4 m = clive ? B.med[ray0 * kGhostD + c] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float2 *line = Ln[warp][half_t][c >> 2];
+        float vv[18];
 #pragma unroll
-  for (int o = 1; o < kGhostD; o <<= 1) {
-    const float px = __shfl_up_sync(0xffffffffu, ax, o), py = __shfl_up_sync(0xffffffffu, ay, o);
-    const float qx = __shfl_up_sync(0xffffffffu, mx, o), qy = __shfl_up_sync(0xffffffffu, my, o);
-    if (j >= o) {
-      // value = a + m * (previous value) with the previous one = p + q * (...)
-      ax = __fmaf_rn(mx, px, ax);
-      ay = __fmaf_rn(my, py, ay);
-      mx *= qx;
-      my *= qy;
+        for (int o = 0; o < 9; ++o) {
+          const int qq = j + o;  // line points j .. j+8; past 7 (beyond the layer): zero
+          const float2 v = (qq < 8 && clive) ? line[qq < 8 ? qq : 7] : make_float2(0.f, 0.f);
+          vv[o] = v.x;
+          vv[9 + o] = v.y;
+        }
+        float s = 0.f;
+#pragma unroll
+        for (int k = 0; k < 18; ++k) s = fmaxf(s, fabsf(vv[k]));
+        s = fmaxf(s, __shfl_xor_sync(0xffffffffu, s, 1));
+        // Stencils this small carry no wave (the first cells a front reaches
+        // hold values near the FP32 underflow, whose reciprocal overflows).
+        if (!(s > kMinScale)) s = 0.f;
+        const float inv = s > 0.f ? 1.0f / s : 0.f;
+        __half *X = Xs[NET ? warp : 0];
+        __half *row = X + c * kXs + 18 * half_t;
+#pragma unroll
+        for (int k = 0; k < 18; k += 2)
+          *reinterpret_cast<__half2 *>(row + k) = __floats2half2_rn(vv[k] * inv, vv[k + 1] * inv);
+        if (half_t == 0) {
+          const int d = G.L - kGhostD + 1 + j;
+          *reinterpret_cast<__half2 *>(X + c * kXs + 36) = __floats2half2_rn(m.x * kVScale, m.y);
+          *reinterpret_cast<__half2 *>(X + c * kXs + 38) = __floats2half2_rn(m.z, (float)d / (float)G.L);
+        } else {
+#pragma unroll
+          for (int k = 40; k < kK1; k += 2) *reinterpret_cast<__half2 *>(X + c * kXs + k) = __floats2half2_rn(0.f, 0.f);
+        }
+        __syncwarp();
+        float ylo[2], yhi[2];
+        mlp16(X, F, ylo, yhi);
+        // Rows g and g + 8 sit in lane 4 g: cell u comes from lane 4 (u % 8).
+        const int src = 4 * (u & 7);
+        const float a0 = __shfl_sync(0xffffffffu, ylo[0], src), a1 = __shfl_sync(0xffffffffu, ylo[1], src);
+        const float b0 = __shfl_sync(0xffffffffu, yhi[0], src), b1 = __shfl_sync(0xffffffffu, yhi[1], src);
+        kc = u < 8 ? make_float2(sigmoid(a0), sigmoid(a1)) : make_float2(sigmoid(b0), sigmoid(b1));
+        if (B.keep && live) B.k[cell] = kc;
+      } else if (live) {
+        kc = B.k[cell];
+      }
+      // 3. the update along each ray (lanes 0 .. 15).
+      const int r = u >> 2, j = u & 3;
+      const float2 cg = Ln[warp][0][r][kGhostD + j];      // the cell at t
+      const float2 ci = Ln[warp][0][r][kGhostD - 1 + j];  // its inward neighbour at t
+      int gidx = 0;
+      float2 ni = make_float2(0.f, 0.f);
+      if (live) {
+        gidx = __float_as_int(B.med[cell].w);
+        if (j == 0) ni = __ldcg(B.next + gidx - (ray0 + r < rmid ? -stride : stride));  // next of d = L-4
+      }
+      // a_d = cur_(d-1) + k_d cur_d, next_d = a_d - k_d next_(d-1): lane j
+      // folds in lanes j-1 .. 0 of its ray (the first one brings next_(L-4)).
+      float ax = __fmaf_rn(kc.x, cg.x, ci.x), ay = __fmaf_rn(kc.y, cg.y, ci.y);
+      float mx = -kc.x, my = -kc.y;  // coefficient of next_(start-1) in the running value
+      if (j == 0) {
+        ax = __fmaf_rn(mx, ni.x, ax);
+        ay = __fmaf_rn(my, ni.y, ay);
+        mx = 0.f;
+        my = 0.f;
+      }
+#pragma unroll
+      for (int o = 1; o < kGhostD; o <<= 1) {
+        const float px = __shfl_up_sync(0xffffffffu, ax, o), py = __shfl_up_sync(0xffffffffu, ay, o);
+        const float qx = __shfl_up_sync(0xffffffffu, mx, o), qy = __shfl_up_sync(0xffffffffu, my, o);
+        if (j >= o) {
+          // value = a + m * (previous value) with the previous one = p + q * (...)
+          ax = __fmaf_rn(mx, px, ax);
+          ay = __fmaf_rn(my, py, ay);
+          mx *= qx;
+          my *= qy;
+        }
+      }
+      if (live) __stcg(B.next + gidx, make_float2(ax, ay));
+      __syncwarp();
     }
+    if (A > 0 && !grid_barrier(B.bar, gridDim.x, B.wait_ns, B.err)) return;
   }
-  if (live) next[gidx] = make_float2(ax, ay);
+}
+
+// The t-1 line points of every ray from the previous field, before the
+// first boundary step (later steps carry them over themselves).
+__global__ void k_abc_lines(const __grid_constant__ Ghost G, const float2 *__restrict__ prev, int sy, int pitch,
+                            const float4 *__restrict__ med, float2 *__restrict__ lines) {
+  const long nrays = G.off[6] / kGhostD;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nrays * 8; i += (long)gridDim.x * blockDim.x) {
+    const long ray = i >> 3;
+    const int q = (int)(i & 7);
+    const int f = face_of(G, ray * kGhostD);
+    const int idx0 = __float_as_int(med[ray * kGhostD].w);
+    lines[i] = prev[idx0 + (q - kGhostD) * normal_step(f, sy, pitch)];
+  }
 }
 
 // Taper of the layer cells after the step: next *= exp(-(damping d)^2).
@@ -955,7 +1006,10 @@ struct ResidentLayer {
   float damping = 0.f;
   Ghost G;
   float4 *med = nullptr;       // medium of every ghost cell (one-way modes)
-  float2 *k = nullptr;         // one-way coefficients of every ghost cell
+  float2 *k = nullptr;         // one-way coefficients of every ghost cell (fixed, or the network's kept ones)
+  float2 *lines[2] = {nullptr, nullptr};  // learned form: t-1 line points of every ray, by step parity
+  unsigned *bar = nullptr;     // the boundary kernel's grid barrier (count, generation)
+  int grid = 0;                // its cooperative grid
   LayerCell *cells = nullptr;  // every layer cell (taper), z, y, x order
   long ncells = 0;
 };
@@ -1030,35 +1084,44 @@ bool abc_active() { return R.on; }
 void abc_release_resident() {
   if (R.med) cudaFree(R.med);
   if (R.k) cudaFree(R.k);
+  if (R.lines[0]) cudaFree(R.lines[0]);
+  if (R.lines[1]) cudaFree(R.lines[1]);
+  if (R.bar) cudaFree(R.bar);
   if (R.cells) cudaFree(R.cells);
   R = ResidentLayer();
 }
 
 int g_interval = 1;  // FLETCHER_AbcSetInterval
 
-cudaError_t abc_before_step(const ResidentView &v) {
-  if (!R.on || R.mode != FLETCHER_BOUNDARY_LEARNED) return cudaSuccess;
-  if (R.steps++ % R.interval != 0) return cudaSuccess;  // the last coefficients stay
-  const long ntiles = (R.G.off[6] + 15) / 16;
-  const long grid = (ntiles + kInferWarps - 1) / kInferWarps;
-  const long cap = v.num_sms > 0 ? (long)v.num_sms * kInferBlocksPerSm : 1024;
-  k_abc_infer<<<(int)(grid < cap ? grid : cap), 32 * kInferWarps, 0, v.stream>>>(R.G, v.cur, v.prev, v.sy, v.pitch,
-                                                                                 R.med, T.net, R.k);
-  return cudaGetLastError();
-}
-
+// After the plain step: the ghost zone's one-way update (with the network
+// on the learned form's evaluation steps) in one cooperative launch, then
+// the taper if any.
 cudaError_t abc_after_step(const ResidentView &v) {
   if (!R.on) return cudaSuccess;
   if (oneway_mode(R.mode)) {
-    // z faces, then y faces, then x faces (edge and corner cells keep the last value).
-    auto grid = [&](int a) {
-      const int t0 = a == 0 ? 1 : 0, t1 = a == 2 ? 1 : 2;
-      const int e0 = R.G.keep.hi[t0] - R.G.keep.lo[t0], e1 = R.G.keep.hi[t1] - R.G.keep.lo[t1];
-      return dim3((unsigned)((e0 * kGhostD + 255) / 256), (unsigned)e1, 2u);
-    };
-    k_abc_rays<2><<<grid(2), 256, 0, v.stream>>>(R.G, v.cur, v.next, v.sy, v.pitch, R.k);
-    k_abc_rays<1><<<grid(1), 256, 0, v.stream>>>(R.G, v.cur, v.next, v.sy, v.pitch, R.k);
-    k_abc_rays<0><<<grid(0), 256, 0, v.stream>>>(R.G, v.cur, v.next, v.sy, v.pitch, R.k);
+    const bool learned = R.mode == FLETCHER_BOUNDARY_LEARNED;
+    BoundaryArgs a;
+    memset(&a, 0, sizeof(a));
+    a.G = R.G;
+    a.cur = v.cur;
+    a.next = v.next;
+    a.sy = v.sy;
+    a.pitch = v.pitch;
+    a.med = R.med;
+    a.net = T.net;
+    a.line_in = R.lines[R.steps & 1];
+    a.line_out = R.lines[(R.steps + 1) & 1];
+    a.k = R.k;
+    a.eval = learned && R.steps % R.interval == 0;  // the last coefficients stay in between
+    a.keep = learned && R.interval > 1;
+    a.bar = R.bar;
+    a.err = v.err;
+    a.wait_ns = kWaitLimitNs;
+    ++R.steps;
+    void *args[] = {&a};
+    const void *kern = learned ? (const void *)k_abc_boundary<true> : (const void *)k_abc_boundary<false>;
+    const cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(R.grid), dim3(32 * kBoundaryWarps), args, 0, v.stream);
+    if (e != cudaSuccess) return e;
   }
   if (R.damping > 0.f && R.ncells)
     k_abc_taper<<<grid_of(R.ncells, 256), 256, 0, v.stream>>>(R.cells, R.ncells, v.next, v.sy, v.pitch, R.damping);
@@ -1294,6 +1357,22 @@ extern "C" int FLETCHER_SetBoundary(int mode, int layer, float damping) {
     k_abc_fill<<<grid_of(n, 256), 256, 0, v.stream>>>(R.G, v.coef, v.sy, v.pitch, v.dt, v.dx, v.dy, v.dz, R.med,
                                                       R.k);
     CKA(cudaGetLastError());
+    if (mode == FLETCHER_BOUNDARY_LEARNED) {
+      // The first step's t-1 lines from the previous field; each boundary
+      // launch then stores the t lines for the next one.
+      for (int b = 0; b < 2; ++b) CKA(cudaMalloc(&R.lines[b], n * 2 * sizeof(float2)));
+      k_abc_lines<<<grid_of(n * 2, 256), 256, 0, v.stream>>>(R.G, v.prev, v.sy, v.pitch, R.med, R.lines[0]);
+      CKA(cudaGetLastError());
+    }
+    CKA(cudaMalloc(&R.bar, 2 * sizeof(unsigned)));
+    CKA(cudaMemsetAsync(R.bar, 0, 2 * sizeof(unsigned), v.stream));
+    // Cooperative grid: every block resident at once (the grid barrier needs it).
+    int per_sm = 0;
+    const void *kern = mode == FLETCHER_BOUNDARY_LEARNED ? (const void *)k_abc_boundary<true>
+                                                         : (const void *)k_abc_boundary<false>;
+    CKA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kBoundaryWarps, 0));
+    if (per_sm < 1) return err(FLETCHER_ERR_CUDA, "SetBoundary: the boundary kernel fits no block on an SM");
+    R.grid = per_sm * (v.num_sms > 0 ? v.num_sms : 1);
   }
   if (damping > 0.f) {
     // Layer cells in z, y, x order (coalesced).

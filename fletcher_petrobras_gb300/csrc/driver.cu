@@ -67,6 +67,7 @@ struct State {
   unsigned *Mx = nullptr;  // [2][sz] plane maxima (float bits) of the field in buffer b
   int ecur = 0;
   HalfMaps hm[2];          // maps of a step whose current field is in buffer b
+  int numerics = FLETCHER_NUMERICS_FAST;
 };
 
 State g;
@@ -93,6 +94,13 @@ int g_errmode = FLETCHER_ERRMODE_EXIT;
 // supports it; 0 (default): device buffers and copies.  On GB300 with Grace
 // the copies measured faster (e2e 66.3 vs 49.2 GMSamples/s at 504^3).
 int g_host_access = 0;
+int g_numerics = FLETCHER_NUMERICS_FAST;
+// Fault injection for the failure-path tests (FLETCHER_InjectFault): the
+// device allocation that fails (counted down, -1: none), and the stall of
+// the next propagate launch (CTA 0's step to skip, -1: none; its wait limit).
+int g_fault_alloc = -1;
+int g_fault_stall = -1;
+unsigned long long g_fault_wait_ns = 0;
 int g_last_err = FLETCHER_OK;
 char g_errmsg[512] = "";
 
@@ -126,6 +134,7 @@ ResidentView resident_view() {
   v.coef = g.coef;
   v.stream = g_stream;
   v.num_sms = g.num_sms;
+  v.err = g.err_dev;
   return v;
 }
 }  // namespace flt
@@ -140,6 +149,19 @@ namespace {
                   "%s failed at %s:%d: %s", #call, __FILE__, __LINE__, cudaGetErrorString(e_));   \
   } while (0)
 
+// Device allocation through the fault-injection countdown.
+cudaError_t dev_malloc(void **p, size_t bytes) {
+  if (g_fault_alloc >= 0 && g_fault_alloc-- == 0) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p, bytes);
+}
+template <class T>
+cudaError_t dev_malloc(T **p, size_t bytes) {
+  return dev_malloc(reinterpret_cast<void **>(p), bytes);
+}
+
 // ---- auxiliary kernels --------------------------------------------------------
 
 // The six raw model arrays (vpz vsv epsilon delta phi theta): device copies,
@@ -148,9 +170,15 @@ struct Raw6 {
   const float *a[6];
 };
 
+// First model value that is not finite, as cell * 8 + array (vpz vsv epsilon
+// delta phi theta); ~0 when every value is finite.  Set by k_precompute.
+__device__ unsigned long long g_bad_model;
+const char *const kModelNames[6] = {"vpz", "vsv", "epsilon", "delta", "phi", "theta"};
+
 // Coefficient precompute, original/precomp.h:14-38 and :49-58: trigonometry
 // in FP64 rounded to float, products of those floats in float, velocity
-// terms in FP64.
+// terms in FP64.  A model value that is not finite is recorded in
+// g_bad_model (the set-up then rejects the model).
 __global__ void k_precompute(Raw6 raw, float *__restrict__ coef, int sx, int sy, int sz, int pitch) {
   const size_t n = (size_t)sx * sy * sz;
   // The trigonometry of the last angles this thread saw: media repeat their
@@ -160,6 +188,13 @@ __global__ void k_precompute(Raw6 raw, float *__restrict__ coef, int sx, int sy,
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const float vpz = raw.a[0][i], vsv = raw.a[1][i], eps = raw.a[2][i], del = raw.a[3][i];
     const float phi = raw.a[4][i], theta = raw.a[5][i];
+    const float in6[6] = {vpz, vsv, eps, del, phi, theta};
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+      if (!isfinite(in6[a])) {
+        atomicMin(&g_bad_model, (unsigned long long)i * 8 + a);
+        break;
+      }
     if (__float_as_int(theta) != __float_as_int(last_theta)) {
       double st, ct;
       sincos((double)theta, &st, &ct);
@@ -541,8 +576,8 @@ int setup_tiles(int rows, int stages) {
   if (g.cta_first) cudaFree(g.cta_first);
   g.seg = nullptr;
   g.cta_first = nullptr;
-  CK(cudaMalloc(&g.seg, sp.seg.size() * sizeof(int4)));
-  CK(cudaMalloc(&g.cta_first, sp.first.size() * sizeof(int)));
+  CK(dev_malloc(&g.seg, sp.seg.size() * sizeof(int4)));
+  CK(dev_malloc(&g.cta_first, sp.first.size() * sizeof(int)));
   CK(cudaMemcpy(g.seg, sp.seg.data(), sp.seg.size() * sizeof(int4), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(g.cta_first, sp.first.data(), sp.first.size() * sizeof(int), cudaMemcpyHostToDevice));
   // CTAs past the last one with work are not launched.
@@ -589,8 +624,13 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   // Default shapes (measured at 504^3): 16 rows; 5 stages for FP32 (2.20 ms
   // per step against 2.40 for 12 x 5) and FP16X (3.45 against 3.68 for 16 x 4),
   // 4 for FP16 (3.02 against 3.18 for 16 x 5).
-  const int rows = g_req_rows ? g_req_rows : 16;
-  const int stages = g_req_stages ? g_req_stages : (g_form == FLETCHER_FORM_FP16 ? 4 : 5);
+  if (g_numerics == FLETCHER_NUMERICS_D1D1 && g_form != FLETCHER_FORM_FP32)
+    return fail(FLETCHER_ERR_ARGS, "the Der1-Der1 numerics need the FP32 form");
+  const bool d1d1 = g_numerics == FLETCHER_NUMERICS_D1D1;
+  if (d1d1 && (g_req_rows || g_req_stages) && (g_req_rows != kD1D1Rows || g_req_stages != kD1D1Stages))
+    return fail(FLETCHER_ERR_ARGS, "the Der1-Der1 numerics run %d x %d tiles only", kD1D1Rows, kD1D1Stages);
+  const int rows = d1d1 ? kD1D1Rows : (g_req_rows ? g_req_rows : 16);
+  const int stages = d1d1 ? kD1D1Stages : (g_req_stages ? g_req_stages : (g_form == FLETCHER_FORM_FP16 ? 4 : 5));
   if (!(half ? propagate_half_supported(rows, stages) : propagate_fp32_supported(rows, stages)))
     return fail(FLETCHER_ERR_ARGS, "tile shape (%d rows, %d stages) is not built for form %d", rows, stages, g_form);
   if (half) {
@@ -627,29 +667,30 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   cudaStream_t s = g_stream;
 
   g.form = g_form;
+  g.numerics = g_numerics;
   if (half) {
     for (int b = 0; b < 2; ++b) {
-      CK(cudaMalloc(&g.Hh[b], g.npitch * sizeof(unsigned)));
+      CK(dev_malloc(&g.Hh[b], g.npitch * sizeof(unsigned)));
       CK(cudaMemsetAsync(g.Hh[b], 0, g.npitch * sizeof(unsigned), s));
       if (ext) {
-        CK(cudaMalloc(&g.Hl[b], g.npitch * sizeof(unsigned short)));
+        CK(dev_malloc(&g.Hl[b], g.npitch * sizeof(unsigned short)));
         CK(cudaMemsetAsync(g.Hl[b], 0, g.npitch * sizeof(unsigned short), s));
       }
     }
-    CK(cudaMalloc(&g.E, 3 * sz * sizeof(int)));
-    CK(cudaMalloc(&g.Mx, 2 * sz * sizeof(unsigned)));
+    CK(dev_malloc(&g.E, 3 * sz * sizeof(int)));
+    CK(dev_malloc(&g.Mx, 2 * sz * sizeof(unsigned)));
     CK(cudaMemsetAsync(g.E, 0, 3 * sz * sizeof(int), s));
     CK(cudaMemsetAsync(g.Mx, 0, 2 * sz * sizeof(unsigned), s));
     g.dev_bytes = 2 * g.npitch * (sizeof(unsigned) + (ext ? sizeof(unsigned short) : 0)) + 5 * sz * sizeof(int);
   } else {
-    CK(cudaMalloc(&g.F[0], g.npitch * sizeof(float2)));
-    CK(cudaMalloc(&g.F[1], g.npitch * sizeof(float2)));
+    CK(dev_malloc(&g.F[0], g.npitch * sizeof(float2)));
+    CK(dev_malloc(&g.F[1], g.npitch * sizeof(float2)));
     CK(cudaMemsetAsync(g.F[0], 0, g.npitch * sizeof(float2), s));
     CK(cudaMemsetAsync(g.F[1], 0, g.npitch * sizeof(float2), s));
     g.dev_bytes = 2 * g.npitch * sizeof(float2);
   }
-  CK(cudaMalloc(&g.coef, g.npitch * kNumCoef * sizeof(float)));
-  CK(cudaMalloc(&g.scratch, g.n * sizeof(float)));
+  CK(dev_malloc(&g.coef, g.npitch * kNumCoef * sizeof(float)));
+  CK(dev_malloc(&g.scratch, g.n * sizeof(float)));
   CK(cudaHostAlloc(&g.err_host, sizeof(unsigned), cudaHostAllocMapped));
   *g.err_host = 0;
   CK(cudaHostGetDevicePointer((void **)&g.err_dev, g.err_host, 0));
@@ -669,7 +710,7 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   if (g.hostmem) {
     for (int k = 0; k < 6; ++k) r6.a[k] = src6[k];
   } else {
-    CK(cudaMalloc(&raw, 6 * g.n * sizeof(float)));
+    CK(dev_malloc(&raw, 6 * g.n * sizeof(float)));
     // Each array is locked while the copies before it run.
     for (int k = 0; k < 6; ++k) {
       pins.add(src6[k], g.n * sizeof(float));
@@ -678,6 +719,8 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
     }
     for (const float *f : {pp, pc, qp, qc}) pins.add(f, g.n * sizeof(float));
   }
+  const unsigned long long all_finite = ~0ull;
+  CK(cudaMemcpyToSymbolAsync(g_bad_model, &all_finite, sizeof(all_finite), 0, cudaMemcpyHostToDevice, s));
   k_precompute<<<grid_for(g.n), 256, 0, s>>>(r6, g.coef, sx, sy, sz, g.pitch);
   CK(cudaGetLastError());
   // Initial fields (the reference's OpenMP back-end works on the caller's
@@ -706,6 +749,11 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   }
   CK(cudaStreamSynchronize(s));
   if (raw) CK(cudaFree(raw));
+  unsigned long long bad = 0;
+  CK(cudaMemcpyFromSymbol(&bad, g_bad_model, sizeof(bad)));
+  if (bad != ~0ull)
+    return fail(FLETCHER_ERR_ARGS, "model array %s holds a value that is not finite at cell %llu", kModelNames[bad % 8],
+                bad / 8);
 
   if (setup_tiles(rows, stages)) return g_last_err;
   g.launches = 0;
@@ -757,6 +805,7 @@ int step() {
   L.stages = g.stages;
   L.grid = g.grid;
   L.batch = false;
+  L.d1d1 = g.numerics == FLETCHER_NUMERICS_D1D1;
   L.m.cur_halo = g.maps.halo[c];
   L.m.prev_pt = g.maps.pt[p];
   L.m.arr = g.maps.arr;
@@ -775,11 +824,20 @@ int step() {
   P.inv_dxx = 1.0f / (g.dx * g.dx);
   P.inv_dyy = 1.0f / (g.dy * g.dy);
   P.inv_dzz = 1.0f / (g.dz * g.dz);
+  P.inv_dxy = 1.0f / (g.dx * g.dy);
+  P.inv_dxz = 1.0f / (g.dx * g.dz);
+  P.inv_dyz = 1.0f / (g.dy * g.dz);
   // On an isotropic grid every derivative carries the same 1/h^2, applied
   // once with the time step; otherwise each derivative is scaled.
   P.iso = (g.dx == g.dy && g.dx == g.dz) ? 1 : 0;
   P.dt2 = P.iso ? (g.dt * g.dt) * P.inv_dxx : g.dt * g.dt;
+  P.dt = g.dt;
   P.err = g.err_dev;
+  // Every wait is bounded (2 s); an injected stall (tests) uses its own limit
+  // and applies to this one launch.
+  P.wait_ns = g_fault_stall >= 0 && g_fault_wait_ns ? g_fault_wait_ns : kWaitLimitNs;
+  P.stall_step = g_fault_stall;
+  g_fault_stall = -1;
   ShotDesc &want = P.one;
   want = g.desc;
   want.src_x = want.src_y = want.src_z = -1000;
@@ -835,7 +893,6 @@ int step() {
     g.ecur = enew;
   } else {
     const bool abc = abc_active();
-    if (abc) CK(abc_before_step(resident_view()));
     CK(propagate_fp32_launch(L, g_stream));
     if (abc) CK(abc_after_step(resident_view()));
   }
@@ -1010,6 +1067,35 @@ extern "C" int FLETCHER_SetForm(int form) {
   return FLETCHER_OK;
 }
 
+extern "C" int FLETCHER_SetNumerics(int mode) {
+  if (mode != FLETCHER_NUMERICS_FAST && mode != FLETCHER_NUMERICS_D1D1)
+    return fail(FLETCHER_ERR_ARGS, "unknown numerics mode %d", mode);
+  g_numerics = mode;
+  return FLETCHER_OK;
+}
+
+extern "C" int FLETCHER_InjectFault(int kind, int arg, int wait_us) {
+  switch (kind) {
+    case FLETCHER_FAULT_NONE:
+      g_fault_alloc = -1;
+      g_fault_stall = -1;
+      g_fault_wait_ns = 0;
+      return FLETCHER_OK;
+    case FLETCHER_FAULT_ALLOC:
+      if (arg < 0) return fail(FLETCHER_ERR_ARGS, "FLETCHER_InjectFault: allocation index must be >= 0");
+      g_fault_alloc = arg;
+      return FLETCHER_OK;
+    case FLETCHER_FAULT_STALL:
+      if (arg < 0 || wait_us < 1000 || wait_us > 2000000)
+        return fail(FLETCHER_ERR_ARGS, "FLETCHER_InjectFault: stall step must be >= 0 and the wait 1 ms .. 2 s");
+      g_fault_stall = arg;
+      g_fault_wait_ns = (unsigned long long)wait_us * 1000ull;
+      return FLETCHER_OK;
+    default:
+      return fail(FLETCHER_ERR_ARGS, "FLETCHER_InjectFault: unknown kind %d", kind);
+  }
+}
+
 extern "C" int FLETCHER_PlanSegments(int ctas, int ntx, int nty, int tile_rows, int zlo, int depth, int zchunks,
                                      int *seg_out, int cap, int *first_out, long *max_cost) {
   if (ctas < 1 || ntx < 1 || nty < 1 || tile_rows < 1 || depth < 1 || cap < 0 || !first_out)
@@ -1129,6 +1215,8 @@ extern "C" int FLETCHER_TuneConfigStore(const char *path, const char *gpu, int s
 
 extern "C" int FLETCHER_Autotune(const char *path, int steps_per_shape) {
   if (!g.init) return fail(FLETCHER_ERR_ARGS, "FLETCHER_Autotune before DRIVER_Initialize");
+  if (g.numerics == FLETCHER_NUMERICS_D1D1)
+    return fail(FLETCHER_ERR_ARGS, "FLETCHER_Autotune: the Der1-Der1 numerics have one tile shape");
   if (!path || strlen(path) >= sizeof(tune.path) || steps_per_shape < 1)
     return fail(FLETCHER_ERR_ARGS, "FLETCHER_Autotune: bad arguments");
   cudaDeviceProp prop;
@@ -1318,16 +1406,16 @@ int batch_seal(int rows, int stages) {
     fill_items(items.data() + base, i, s.ntx, s.nty, s.nchunk, rows);
     B.items_upto[oi] = (int)items.size();
   }
-  CK(cudaMalloc(&B.d_desc, sizeof(ShotDesc) * ns));
-  CK(cudaMalloc(&B.d_maps, sizeof(ShotMaps) * ns));
-  CK(cudaMalloc(&B.d_items, sizeof(int4) * items.size()));
+  CK(dev_malloc(&B.d_desc, sizeof(ShotDesc) * ns));
+  CK(dev_malloc(&B.d_maps, sizeof(ShotMaps) * ns));
+  CK(dev_malloc(&B.d_items, sizeof(int4) * items.size()));
   CK(cudaMemcpy(B.d_desc, desc.data(), sizeof(ShotDesc) * ns, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(B.d_maps, maps.data(), sizeof(ShotMaps) * ns, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(B.d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
   if (batch_half()) {
-    CK(cudaMalloc(&B.d_hshots, sizeof(HalfShot) * ns));
-    CK(cudaMalloc(&B.d_hmaps, sizeof(HalfShotMaps) * ns));
-    CK(cudaMalloc(&B.d_order, sizeof(int) * ns));
+    CK(dev_malloc(&B.d_hshots, sizeof(HalfShot) * ns));
+    CK(dev_malloc(&B.d_hmaps, sizeof(HalfShotMaps) * ns));
+    CK(dev_malloc(&B.d_order, sizeof(int) * ns));
     CK(cudaMemcpy(B.d_hshots, hshots.data(), sizeof(HalfShot) * ns, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(B.d_hmaps, hmaps.data(), sizeof(HalfShotMaps) * ns, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(B.d_order, B.order.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
@@ -1349,6 +1437,8 @@ int batch_issue(int it0, int it1, const float *src) {
   PropLaunch L;
   memset(&L, 0, sizeof(L));
   L.batch = true;
+  L.p.wait_ns = kWaitLimitNs;
+  L.p.stall_step = -1;
   L.tile_rows = B.sealed_rows;
   L.stages = B.stages;
   PropParams &P = L.p;
@@ -1361,8 +1451,12 @@ int batch_issue(int it0, int it1, const float *src) {
   P.inv_dxx = 1.0f / (B.dx * B.dx);
   P.inv_dyy = 1.0f / (B.dy * B.dy);
   P.inv_dzz = 1.0f / (B.dz * B.dz);
+  P.inv_dxy = 1.0f / (B.dx * B.dy);
+  P.inv_dxz = 1.0f / (B.dx * B.dz);
+  P.inv_dyz = 1.0f / (B.dy * B.dz);
   P.iso = (B.dx == B.dy && B.dx == B.dz) ? 1 : 0;
   P.dt2 = P.iso ? (B.dt * B.dt) * P.inv_dxx : B.dt * B.dt;
+  P.dt = B.dt;
   P.err = B.err_dev;
   const int ctas = B.ctas;
   int active = ns;  // shots still running, a prefix of B.order
@@ -1444,19 +1538,19 @@ extern "C" int FLETCHER_BatchAddShot(int sx, int sy, int sz, const float *model,
   bool ok = true;
   for (int b = 0; b < 2; ++b) {
     if (half) {
-      ok = ok && cudaMalloc(&s.Hh[b], fbytes) == cudaSuccess;
-      if (ext) ok = ok && cudaMalloc(&s.Hl[b], s.npitch * sizeof(unsigned short)) == cudaSuccess;
+      ok = ok && dev_malloc(&s.Hh[b], fbytes) == cudaSuccess;
+      if (ext) ok = ok && dev_malloc(&s.Hl[b], s.npitch * sizeof(unsigned short)) == cudaSuccess;
     } else {
-      ok = ok && cudaMalloc(&s.F[b], fbytes) == cudaSuccess;
+      ok = ok && dev_malloc(&s.F[b], fbytes) == cudaSuccess;
     }
   }
   if (half) {
-    ok = ok && cudaMalloc(&s.E, 3 * sz * sizeof(int)) == cudaSuccess;
-    ok = ok && cudaMalloc(&s.Mx, 2 * sz * sizeof(unsigned)) == cudaSuccess;
+    ok = ok && dev_malloc(&s.E, 3 * sz * sizeof(int)) == cudaSuccess;
+    ok = ok && dev_malloc(&s.Mx, 2 * sz * sizeof(unsigned)) == cudaSuccess;
   }
-  ok = ok && cudaMalloc(&s.coef, s.npitch * kNumCoef * sizeof(float)) == cudaSuccess;
+  ok = ok && dev_malloc(&s.coef, s.npitch * kNumCoef * sizeof(float)) == cudaSuccess;
   float *raw = nullptr;
-  ok = ok && cudaMalloc(&raw, 6 * s.n * sizeof(float)) == cudaSuccess;
+  ok = ok && dev_malloc(&raw, 6 * s.n * sizeof(float)) == cudaSuccess;
   auto release = [&]() {
     for (int b = 0; b < 2; ++b) {
       if (s.F[b]) cudaFree(s.F[b]);
@@ -1477,6 +1571,9 @@ extern "C" int FLETCHER_BatchAddShot(int sx, int sy, int sz, const float *model,
   pin.add(model, 6 * s.n * sizeof(float));
   cudaError_t e = cudaMemcpyAsync(raw, model, 6 * s.n * sizeof(float), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(s.coef, 0, s.npitch * kNumCoef * sizeof(float), st);
+  const unsigned long long all_finite = ~0ull;
+  if (e == cudaSuccess)
+    e = cudaMemcpyToSymbolAsync(g_bad_model, &all_finite, sizeof(all_finite), 0, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     Raw6 r6;
     for (int k = 0; k < 6; ++k) r6.a[k] = raw + k * s.n;
@@ -1496,12 +1593,20 @@ extern "C" int FLETCHER_BatchAddShot(int sx, int sy, int sz, const float *model,
     release();
     return -fail(FLETCHER_ERR_CUDA, "shot set-up: %s", cudaGetErrorString(e));
   }
+  unsigned long long bad = 0;
+  e = cudaMemcpyFromSymbol(&bad, g_bad_model, sizeof(bad));
+  if (e != cudaSuccess || bad != ~0ull) {
+    release();
+    if (e != cudaSuccess) return -fail(FLETCHER_ERR_CUDA, "shot set-up: %s", cudaGetErrorString(e));
+    return -fail(FLETCHER_ERR_ARGS, "shot %zu: model array %s holds a value that is not finite at cell %llu",
+                 B.shots.size(), kModelNames[bad % 8], bad / 8);
+  }
   B.dev_bytes += 2 * fbytes + s.npitch * kNumCoef * sizeof(float);
   if (half) B.dev_bytes += (ext ? 2 * s.npitch * sizeof(unsigned short) : 0) + 5 * sz * sizeof(int);
   if (s.n > B.max_n) {
     if (B.scratch) cudaFree(B.scratch);
     B.scratch = nullptr;
-    if (cudaMalloc(&B.scratch, s.n * sizeof(float)) != cudaSuccess) {
+    if (dev_malloc(&B.scratch, s.n * sizeof(float)) != cudaSuccess) {
       cudaGetLastError();
       return -fail(FLETCHER_ERR_NOMEM, "read-back buffer allocation failed");
     }

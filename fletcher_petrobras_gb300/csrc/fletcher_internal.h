@@ -57,13 +57,17 @@ struct PropParams {
   int parity;                       // current field = F[parity], previous = F[1 - parity]
   float inv_dx, inv_dy, inv_dz;     // 1/dx, 1/dy, 1/dz
   float inv_dxx, inv_dyy, inv_dzz;  // 1/(dx*dx), 1/(dy*dy), 1/(dz*dz) as the reference forms them
+  float inv_dxy, inv_dxz, inv_dyz;  // 1/(dx*dy), 1/(dx*dz), 1/(dy*dz): factors of the cross derivatives
   int iso;                          // dx == dy == dz: derivatives unscaled, dt2 = dt^2 / h^2
   float dt2;                        // factor of the rhs in the update
+  float dt;                         // the time step (Der1-Der1 numerics: rhs * dt * dt)
   float src;                        // value added at each shot's source cell (src_z >= 0)
   float cor;                        // value owed at each shot's cor cell (cor_z >= 0)
   unsigned int *err;                // error word (bit 0: bounded wait gave up)
   const int4 *seg;                  // single-shot launches with a segment list
   const int *cta_first;             // their [grid + 1] first segments
+  unsigned long long wait_ns;       // limit of the step's waits (ns)
+  int stall_step;                   // test hook: CTA 0 skips the loads of its stall_step-th step (-1: none)
 };
 
 // The four descriptors a single-shot launch passes as kernel parameters.
@@ -75,6 +79,7 @@ struct PropLaunch {
   PropParams p;
   SingleMaps m;           // single-shot launches
   bool batch;             // true: p.shots / p.maps / p.items describe the work
+  bool d1d1;              // Der1-Der1 numerics (single shot, 16 x 4 tiles)
   int tile_rows;          // TY
   int stages;
   int grid;
@@ -86,6 +91,8 @@ int propagate_fp32_threads(int tile_rows);
 int propagate_fp32_ctas_per_sm(int tile_rows);
 cudaError_t propagate_fp32_prepare(int tile_rows, int stages);
 cudaError_t propagate_fp32_launch(const PropLaunch &L, cudaStream_t s);
+// Tile shape of the Der1-Der1 numerics (the only one built for it).
+constexpr int kD1D1Rows = 16, kD1D1Stages = 4;
 
 // ---- 16-bit field storage (propagate_half.cu) ----
 // A field buffer holds (p, q) as half2 per cell ([z][y][pitch]) and, in the
@@ -158,11 +165,11 @@ struct ResidentView {
   const float *coef = nullptr;                   // [z][10][y][pitch] (DevCoef order)
   cudaStream_t stream = nullptr;
   int num_sms = 0;
+  unsigned *err = nullptr;                       // the error word (bit 0: a bounded wait gave up)
 };
 ResidentView resident_view();       // driver.cu; cur/prev/next for the next step
-bool abc_active();                  // a learned layer is set on the resident state
-cudaError_t abc_before_step(const ResidentView &v);  // layer corrections from cur and prev
-cudaError_t abc_after_step(const ResidentView &v);   // adds them into next
+bool abc_active();                  // a boundary layer is set on the resident state
+cudaError_t abc_after_step(const ResidentView &v);   // the layer's update of next, after the plain step
 void abc_release_resident();        // the resident state is re-initialised or finalised
 
 // ---- output path (snapshot.cu) ----

@@ -34,7 +34,7 @@
 
 namespace flt {
 
-template <int TY>
+template <int TY, bool D1D1 = false>
 struct Geo {
   static constexpr int TX = kTileX;
   static constexpr int HX = TX + 2 * kRadius;
@@ -48,19 +48,25 @@ struct Geo {
   static constexpr int OFF_UPD = OFF_ARR + ARR_B;
   static constexpr int OFF_PP = OFF_UPD + UPD_B;
   static constexpr int STAGE_B = (OFF_PP + PP_B + 127) / 128 * 128;
-  static constexpr int DBUF_B = 2 * TY * HX * 8;  // D1y rows with their x halo, double-buffered
+  // Exchange buffer, double-buffered: D1y of the tile rows with their 4-column
+  // x halo, or (Der1-Der1 numerics) D1x of the tile columns with their 4-row
+  // y halo.
+  static constexpr int DBUF_B = D1D1 ? 2 * HY * TX * 8 : 2 * TY * HX * 8;
   // Tiles of 16 rows (512 threads, at most 128 registers a thread), and of 8
-  // rows (two CTAs per SM), keep the per-cell in-plane terms (A, B) of the
-  // last 5 planes in shared memory instead of a 9-plane register ring.
+  // rows (two CTAs per SM), keep the per-cell in-plane terms (A, B; and C
+  // for the Der1-Der1 numerics) of the last 5 planes in shared memory
+  // instead of a 9-plane register ring.
   static constexpr bool AB_SMEM = TY >= 16 || TY <= 8;  // 8 rows run two CTAs per SM (128 registers)
-  static constexpr int AB_B = AB_SMEM ? 5 * NT * 16 : 0;
+  static constexpr int AB_B = AB_SMEM ? 5 * NT * (D1D1 ? 24 : 16) : 0;
   static_assert(TY % 4 == 0, "tile rows must be a multiple of 4");
+  static_assert(!D1D1 || (AB_SMEM && TY >= 8), "the Der1-Der1 numerics keep their in-plane terms in shared memory");
   static_assert(HALO_B % 128 == 0 && ARR_B % 128 == 0 && UPD_B % 128 == 0, "stage regions 128-B aligned");
 };
 
-template <int TY, int S>
+template <int TY, int S, bool D1D1 = false>
 constexpr size_t smem_bytes() {
-  return size_t(S) * Geo<TY>::STAGE_B + Geo<TY>::DBUF_B + Geo<TY>::AB_B + 8 * S + 8 + 16 + 64 + 128;
+  using G = Geo<TY, D1D1>;
+  return size_t(S) * G::STAGE_B + G::DBUF_B + G::AB_B + 8 * S + 8 + 16 + 64 + 128;
 }
 
 // A work item resolved against its shot: tile origin, z range, and (batched
@@ -131,6 +137,7 @@ struct StepMaps {
 struct Cursor {
   Item it;
   int item, k, stage;
+  int n;  // steps issued so far by this CTA
 };
 
 // Issues the TMA loads of one step (plane k of item `it`) into `stage`.
@@ -150,17 +157,22 @@ __device__ __forceinline__ void issue_step(unsigned char *stage, uint64_t *bar, 
   }
 }
 
-template <int TY, int S, bool ISO, int MODE, int MINB>
+// D1D1: the Der1-Der1 numerics.  HOOK: the fault-injection variant (waits
+// limited to P.wait_ns, CTA 0 skipping the loads of step P.stall_step),
+// launched only when a test injects a stall.
+template <int TY, int S, bool ISO, int MODE, int MINB, bool D1D1 = false, bool HOOK = false>
 __global__ void __launch_bounds__(kTileX *TY, MINB)
     k_propagate_fp32(const __grid_constant__ SingleMaps SM, const __grid_constant__ PropParams P) {
   constexpr bool BATCH = MODE == kItemsBatch;
-  using G = Geo<TY>;
+  static_assert(!D1D1 || (!ISO && !BATCH), "the Der1-Der1 numerics scale every derivative, single shot only");
+  using G = Geo<TY, D1D1>;
   extern __shared__ unsigned char smem_dyn[];
   // Align in the shared window (pointer arithmetic on the shared array keeps
   // every access below a shared-memory access).
   unsigned char *smem = smem_dyn + ((128u - (smem_addr(smem_dyn) & 127u)) & 127u);
   f2 *dbuf = reinterpret_cast<f2 *>(smem + S * G::STAGE_B);
   float4 *ABs = reinterpret_cast<float4 *>(smem + S * G::STAGE_B + G::DBUF_B);  // [5][NT] (AB_SMEM)
+  f2 *Cs = reinterpret_cast<f2 *>(ABs + 5 * G::NT);  // [5][NT] (Der1-Der1 numerics: ch1dxy * pxy)
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + S * G::STAGE_B + G::DBUF_B + G::AB_B);
   uint64_t *xchg = full + S;  // D1y rows written (one arrival per warp)
   int *s_abort = reinterpret_cast<int *>(xchg + 1);
@@ -196,10 +208,14 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
     return m;
   };
   Cursor *cur = reinterpret_cast<Cursor *>(s_abort + 4);
-  // Issues the cursor's step into its stage and advances the cursor.
+  // Issues the cursor's step into its stage and advances the cursor.  (Test
+  // hook: CTA 0 skips the loads of its P.stall_step-th step, so that the
+  // waits for that stage give up and the launch reports a timeout.)
   auto produce = [&]() {
     Cursor c = *cur;
-    issue_step<TY>(smem + c.stage * G::STAGE_B, &full[c.stage], c.it, c.k, maps_of(c.it));
+    if (!HOOK || c.n != P.stall_step || blockIdx.x != 0)
+      issue_step<TY>(smem + c.stage * G::STAGE_B, &full[c.stage], c.it, c.k, maps_of(c.it));
+    if constexpr (HOOK) ++c.n;
     if (++c.stage == S) c.stage = 0;
     if (++c.k >= c.it.z1 + kRadius) {
       c.item += item_step();
@@ -223,6 +239,7 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
     c.item = R.first;
     c.k = c.it.z0 - kRadius;
     c.stage = 0;
+    c.n = 0;
     *cur = c;
   }
   __syncthreads();
@@ -238,8 +255,9 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
     for (int a = 0; a < S - 2 && cur->item < item_end(); ++a) produce();
   }
 
+  const uint64_t wait_ns = HOOK ? P.wait_ns : kWaitLimitNs;
   // Spacing factors (unused on isotropic grids).
-  const float sx1 = P.inv_dx, sy1 = P.inv_dy, sz1 = P.inv_dz;
+  const float sxy = P.inv_dxy, sxz = P.inv_dxz, syz = P.inv_dyz;
   const float sxx = P.inv_dxx, syy = P.inv_dyy, szz = P.inv_dzz;
   // Halo-column duty: warps 0 .. TY/4-1 evaluate D1y in the 4 columns left
   // and right of the tile for all TY rows (lane -> row 4*warp + lane/8).
@@ -275,7 +293,7 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
         const int k = kb + j;
         if (k >= kend) break;
         unsigned char *st = smem + stage * G::STAGE_B;
-        if (!mbar_wait(&full[stage], phase, kWaitLimitNs)) {
+        if (!mbar_wait(&full[stage], phase, wait_ns)) {
           *s_abort = 1;
           atomicOr(P.err, 1u);
           goto aborted;
@@ -304,14 +322,44 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
           if (gy == src_y && abs(src_x - gx) <= kRadius) add_at(c, xa, xb, src_x - gx, sv);
           if (gx == src_x && src_y != gy && abs(src_y - gy) <= kRadius) add_at(dummy, ya, yb, src_y - gy, sv);
         }
-        const f2 d1x = scale<ISO>(d1(xa[0], xb[0], xa[1], xb[1], xa[2], xb[2], xa[3], xb[3]), sx1);
-        const f2 d1y = scale<ISO>(d1(ya[0], yb[0], ya[1], yb[1], ya[2], yb[2], ya[3], yb[3]), sy1);
+        f2 d1x, d1y;
+        if constexpr (D1D1) {
+          // der1der1/sample.h:35-49: pDx = Der1_x(p) / dx and pDy = Der1_y(p) / dy.
+          d1x = d1_ref(xa[0], xb[0], xa[1], xb[1], xa[2], xb[2], xa[3], xb[3], P.inv_dx);
+          d1y = d1_ref(ya[0], yb[0], ya[1], yb[1], ya[2], yb[2], ya[3], yb[3], P.inv_dy);
+        } else {
+          d1x = d1(xa[0], xb[0], xa[1], xb[1], xa[2], xb[2], xa[3], xb[3]);
+          d1y = d1(ya[0], yb[0], ya[1], yb[1], ya[2], yb[2], ya[3], yb[3]);
+        }
         Pr[j] = c;
         Dx[j] = d1x;
         Dy[j] = d1y;
         f2 d2x, d2y;
-        f2 *db = dbuf + dsel * (TY * G::HX);
-        if (center) {
+        constexpr int DB_N = D1D1 ? G::HY * G::TX : TY * G::HX;
+        f2 *db = dbuf + dsel * DB_N;
+        if constexpr (D1D1) {
+          if (center) {
+            d2x = d2_ref(c, xa[0], xb[0], xa[1], xb[1], xa[2], xb[2], xa[3], xb[3], sxx);
+            d2y = d2_ref(c, ya[0], yb[0], ya[1], yb[1], ya[2], yb[2], ya[3], yb[3], syy);
+            // pDx of the tile column and of its 4-row y halo: the row's own
+            // value, and warps 0..7 one halo row each (halo-tile rows 0..3 and
+            // TY+4..TY+7).
+            db[(ly + kRadius) * G::TX + lx] = d1x;
+            if (ly < 2 * kRadius) {
+              const int hrow = ly < kRadius ? ly : TY + ly;
+              const int hb0 = hrow * G::HX + lx + kRadius;
+              f2 ha[4], hb[4], dummy;
+#pragma unroll
+              for (int o = 1; o <= 4; ++o) {
+                ha[o - 1] = H[hb0 + o];
+                hb[o - 1] = H[hb0 - o];
+              }
+              if (src_plane && it.y0 - kRadius + hrow == sd.src_y && abs(sd.src_x - gx) <= kRadius)
+                add_at(dummy, ha, hb, sd.src_x - gx, splat(P.src));
+              db[hrow * G::TX + lx] = d1_ref(ha[0], hb[0], ha[1], hb[1], ha[2], hb[2], ha[3], hb[3], P.inv_dx);
+            }
+          }
+        } else if (center) {
           d2x = scale<ISO>(d2(c, xa[0], xb[0], xa[1], xb[1], xa[2], xb[2], xa[3], xb[3]), sxx);
           d2y = scale<ISO>(d2(c, ya[0], yb[0], ya[1], yb[1], ya[2], yb[2], ya[3], yb[3]), syy);
           db[ly * G::HX + lx + kRadius] = d1y;
@@ -330,7 +378,7 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
                 add_at(dummy, ha, hb, src_y - hgy, splat(P.src));
               }
             }
-            db[hr * G::HX + hxc] = scale<ISO>(d1(ha[0], hb[0], ha[1], hb[1], ha[2], hb[2], ha[3], hb[3]), sy1);
+            db[hr * G::HX + hxc] = d1(ha[0], hb[0], ha[1], hb[1], ha[2], hb[2], ha[3], hb[3]);
           }
         }
         // Split-phase exchange: announce this warp's D1y (and, by program
@@ -350,9 +398,17 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
 #define RP(o) Pr[(cs + (o)) % 9]
 #define RX(o) Dx[(cs + (o)) % 9]
 #define RY(o) Dy[(cs + (o)) % 9]
-          const f2 d2z = scale<ISO>(d2(RP(0), RP(1), RP(8), RP(2), RP(7), RP(3), RP(6), RP(4), RP(5)), szz);
-          const f2 dxz = scale<ISO>(d1(RX(1), RX(8), RX(2), RX(7), RX(3), RX(6), RX(4), RX(5)), sz1);
-          const f2 dyz = scale<ISO>(d1(RY(1), RY(8), RY(2), RY(7), RY(3), RY(6), RY(4), RY(5)), sz1);
+          f2 d2z, dxz, dyz;
+          if constexpr (D1D1) {
+            // der1der1/sample.h:58-66: pzz, pxz = Der1_z(pDx) / dz, pyz = Der1_z(pDy) / dz.
+            d2z = d2_ref(RP(0), RP(1), RP(8), RP(2), RP(7), RP(3), RP(6), RP(4), RP(5), szz);
+            dxz = d1_ref(RX(1), RX(8), RX(2), RX(7), RX(3), RX(6), RX(4), RX(5), P.inv_dz);
+            dyz = d1_ref(RY(1), RY(8), RY(2), RY(7), RY(3), RY(6), RY(4), RY(5), P.inv_dz);
+          } else {
+            d2z = scale<ISO>(d2(RP(0), RP(1), RP(8), RP(2), RP(7), RP(3), RP(6), RP(4), RP(5)), szz);
+            dxz = scale<ISO>(d1(RX(1), RX(8), RX(2), RX(7), RX(3), RX(6), RX(4), RX(5)), sxz);
+            dyz = scale<ISO>(d1(RY(1), RY(8), RY(2), RY(7), RY(3), RY(6), RY(4), RY(5)), syz);
+          }
 #undef RP
 #undef RX
 #undef RY
@@ -369,23 +425,44 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
             Ak = A[cs];
             Bk = B[cs];
           }
-          const f2 h1 = fma2(splat(cyz), dyz, fma2(splat(cxz), dxz, fma2(splat(czz), d2z, Ak)));
-          const f2 h2 = sub2(add2(Bk, d2z), h1);
-          const float h1p = lo(h1), h1q = hi(h1), h2p = lo(h2), h2q = hi(h2);
-          // Explicit roundings: every unrolled copy computes identical floats.
-          const float t = __fmul_rn(v2pz, h1q);
-          const float rhsp = __fmaf_rn(v2sz, __fsub_rn(h1p, h1q), __fmaf_rn(v2px, h2p, t));
-          const float rhsq = __fmaf_rn(-v2sz, __fsub_rn(h2p, h2q), __fmaf_rn(v2pn, h2p, t));
+          f2 h1, h2;
+          float rhsp, rhsq;
+          if constexpr (D1D1) {
+            // der1der1/sample.h:70-117 in its order, each operation rounded:
+            // h1 = cpxx + cpyy + cpzz + cpxy + cpxz + cpyz (A = cpxx + cpyy,
+            // C = cpxy from the plane's arrival), h2 = pxx + pyy + pzz - h1.
+            const f2 Ck = Cs[(abw == 4 ? 0 : abw + 1) * G::NT + ci];
+            h1 = add_rn(add_rn(add_rn(add_rn(Ak, mul_rn(czz, d2z)), Ck), mul_rn(cxz, dxz)), mul_rn(cyz, dyz));
+            h2 = sub_rn(add_rn(Bk, d2z), h1);
+            const float h1p = lo(h1), h1q = hi(h1), h2p = lo(h2), h2q = hi(h2);
+            const float t = __fmul_rn(v2pz, h1q);
+            rhsp = __fadd_rn(__fadd_rn(__fmul_rn(v2px, h2p), t), __fmul_rn(v2sz, __fsub_rn(h1p, h1q)));
+            rhsq = __fsub_rn(__fadd_rn(__fmul_rn(v2pn, h2p), t), __fmul_rn(v2sz, __fsub_rn(h2p, h2q)));
+          } else {
+            h1 = fma2(splat(cyz), dyz, fma2(splat(cxz), dxz, fma2(splat(czz), d2z, Ak)));
+            h2 = sub2(add2(Bk, d2z), h1);
+            const float h1p = lo(h1), h1q = hi(h1), h2p = lo(h2), h2q = hi(h2);
+            // Explicit roundings: every unrolled copy computes identical floats.
+            const float t = __fmul_rn(v2pz, h1q);
+            rhsp = __fmaf_rn(v2sz, __fsub_rn(h1p, h1q), __fmaf_rn(v2px, h2p, t));
+            rhsq = __fmaf_rn(-v2sz, __fsub_rn(h2p, h2q), __fmaf_rn(v2pn, h2p, t));
+          }
           f2 old = reinterpret_cast<const f2 *>(st + G::OFF_PP)[ci];
           const int zc = k - kRadius;
           if (zc == cor_z) {
             if (gx == sd.cor_x && gy == sd.cor_y) old = add2(old, splat(P.cor));
           }
           const f2 cur = Pr[cs];
-          const f2 nw = fma2(mk2(rhsp, rhsq), splat(P.dt2), sub2(add2(cur, cur), old));
+          f2 nw;
+          if constexpr (D1D1) {
+            // pp = 2 pc - pp + rhs * dt * dt (der1der1/sample.h:119-120).
+            nw = add_rn(sub_rn(add_rn(cur, cur), old), mul_rn(P.dt, mul_rn(P.dt, mk2(rhsp, rhsq))));
+          } else {
+            nw = fma2(mk2(rhsp, rhsq), splat(P.dt2), sub2(add2(cur, cur), old));
+          }
           if (valid) out[(long)zc * plane] = nw.v;
         }
-        if (!mbar_wait(xchg, xphase, kWaitLimitNs)) {
+        if (!mbar_wait(xchg, xphase, wait_ns)) {
           // A warp of this CTA stopped arriving (it gave up a wait itself):
           // leave too, so that no thread keeps waiting step after step.
           *s_abort = 1;
@@ -393,9 +470,24 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
           goto aborted;
         }
         xphase ^= 1u;
-        if (center) {
+        if constexpr (D1D1) {
+          if (center) {
+            // pxy = Der1_y(pDx) / dy (der1der1/sample.h:55); A = cpxx + cpyy,
+            // B = pxx + pyy, C = cpxy.
+            const f2 *dc = db + (ly + kRadius) * G::TX + lx;
+            constexpr int W = G::TX;
+            const f2 pxy = d1_ref(dc[W], dc[-W], dc[2 * W], dc[-2 * W], dc[3 * W], dc[-3 * W], dc[4 * W], dc[-4 * W],
+                                  P.inv_dy);
+            const float *ca = reinterpret_cast<const float *>(st + G::OFF_ARR);
+            const float cxx = ca[ci], cyy = ca[G::NT + ci], cxy = ca[2 * G::NT + ci];
+            const f2 av = add_rn(mul_rn(cxx, d2x), mul_rn(cyy, d2y));
+            const f2 bv = add_rn(d2x, d2y);
+            ABs[abw * G::NT + ci] = make_float4(lo(av), hi(av), lo(bv), hi(bv));
+            Cs[abw * G::NT + ci] = mul_rn(cxy, pxy);
+          }
+        } else if (center) {
           const f2 *dr = db + ly * G::HX + lx + kRadius;
-          const f2 dxy = scale<ISO>(d1(dr[1], dr[-1], dr[2], dr[-2], dr[3], dr[-3], dr[4], dr[-4]), sx1);
+          const f2 dxy = scale<ISO>(d1(dr[1], dr[-1], dr[2], dr[-2], dr[3], dr[-3], dr[4], dr[-4]), sxy);
           const float *ca = reinterpret_cast<const float *>(st + G::OFF_ARR);
           const float cxx = ca[ci], cyy = ca[G::NT + ci], cxy = ca[2 * G::NT + ci];
           const f2 av = fma2(splat(cxy), dxy, fma2(splat(cyy), d2y, mul2(splat(cxx), d2x)));
@@ -487,7 +579,52 @@ cudaError_t propagate_fp32_prepare(int ty, int st) {
   return cudaErrorInvalidValue;
 }
 
+// The Der1-Der1 numerics: one shape (kD1D1Rows x kD1D1Stages), single shot.
+static cudaError_t launch_d1d1(const PropLaunch &L, cudaStream_t s) {
+  constexpr int TY = kD1D1Rows, S = kD1D1Stages;
+  constexpr size_t smem = smem_bytes<TY, S, true>();
+  static_assert(smem <= 227 * 1024, "Der1-Der1 shape exceeds the shared memory of a CTA");
+  auto tiles = k_propagate_fp32<TY, S, false, kItemsTiles, 1, true>;
+  auto segs = k_propagate_fp32<TY, S, false, kItemsSegments, 1, true>;
+  static bool ready = false;
+  if (!ready) {
+    for (auto kern : {tiles, segs}) {
+      const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    ready = true;
+  }
+  if (L.batch || L.tile_rows != TY || L.stages != S) return cudaErrorInvalidValue;
+  (L.p.seg ? segs : tiles)<<<L.grid, kTileX * TY, smem, s>>>(L.m, L.p);
+  return cudaGetLastError();
+}
+
+// The fault-injection variant: the default shape, single shot.
+static cudaError_t launch_hook(const PropLaunch &L, cudaStream_t s) {
+  constexpr int TY = 16, S = 5;
+  constexpr size_t smem = smem_bytes<TY, S>();
+  auto tiles_i = k_propagate_fp32<TY, S, true, kItemsTiles, 1, false, true>;
+  auto tiles_a = k_propagate_fp32<TY, S, false, kItemsTiles, 1, false, true>;
+  auto segs_i = k_propagate_fp32<TY, S, true, kItemsSegments, 1, false, true>;
+  auto segs_a = k_propagate_fp32<TY, S, false, kItemsSegments, 1, false, true>;
+  static bool ready = false;
+  if (!ready) {
+    for (auto kern : {tiles_i, tiles_a, segs_i, segs_a}) {
+      const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    ready = true;
+  }
+  if (L.batch || L.d1d1 || L.tile_rows != TY || L.stages != S) return cudaErrorInvalidValue;
+  const bool iso = L.p.iso != 0;
+  auto kern = L.p.seg ? (iso ? segs_i : segs_a) : (iso ? tiles_i : tiles_a);
+  kern<<<L.grid, kTileX * TY, smem, s>>>(L.m, L.p);
+  return cudaGetLastError();
+}
+
 cudaError_t propagate_fp32_launch(const PropLaunch &L, cudaStream_t s) {
+  if (L.p.stall_step >= 0) return launch_hook(L, s);
+  if (L.d1d1) return launch_d1d1(L, s);
 #define X(a, b, c) \
   if (L.tile_rows == a && L.stages == b) return launch_t<a, b, c>(L, s);
   FLT_SHAPES(X)

@@ -27,6 +27,33 @@ __device__ __forceinline__ f2 d2(f2 c, f2 a1, f2 b1, f2 a2, f2 b2, f2 a3, f2 b3,
   r = fma2(splat(cK3), add2(a3, b3), r);
   return fma2(splat(cK4), add2(a4, b4), r);
 }
+// (p, q) pairs through the scalar round-to-nearest intrinsics: each
+// operation rounded on its own, never contracted into a fused multiply-add
+// (unlike plain expressions, which the compiler may fuse).
+__device__ __forceinline__ f2 add_rn(f2 a, f2 b) { return mk2(__fadd_rn(lo(a), lo(b)), __fadd_rn(hi(a), hi(b))); }
+__device__ __forceinline__ f2 sub_rn(f2 a, f2 b) { return mk2(__fsub_rn(lo(a), lo(b)), __fsub_rn(hi(a), hi(b))); }
+__device__ __forceinline__ f2 mul_rn(float s, f2 b) { return mk2(__fmul_rn(s, lo(b)), __fmul_rn(s, hi(b))); }
+
+// The two derivatives in the reference's operation order
+// (original/derivatives.h:47,53, the Der1 / Der2 macros): every term
+// rounded on its own, the terms summed left to right, the sum multiplied by
+// the inverse spacing last -- the floats of a build without contraction.
+__device__ __forceinline__ f2 d1_ref(f2 a1, f2 b1, f2 a2, f2 b2, f2 a3, f2 b3, f2 a4, f2 b4, float dinv) {
+  f2 r = mul_rn(cL1, sub_rn(a1, b1));
+  r = add_rn(r, mul_rn(cL2, sub_rn(a2, b2)));
+  r = add_rn(r, mul_rn(cL3, sub_rn(a3, b3)));
+  r = add_rn(r, mul_rn(cL4, sub_rn(a4, b4)));
+  return mul_rn(dinv, r);
+}
+__device__ __forceinline__ f2 d2_ref(f2 c, f2 a1, f2 b1, f2 a2, f2 b2, f2 a3, f2 b3, f2 a4, f2 b4, float d2inv) {
+  f2 r = mul_rn(cK0, c);
+  r = add_rn(r, mul_rn(cK1, add_rn(a1, b1)));
+  r = add_rn(r, mul_rn(cK2, add_rn(a2, b2)));
+  r = add_rn(r, mul_rn(cK3, add_rn(a3, b3)));
+  r = add_rn(r, mul_rn(cK4, add_rn(a4, b4)));
+  return mul_rn(d2inv, r);
+}
+
 // Applies a spacing factor unless the grid is isotropic (then every factor
 // is folded into one dt^2/h^2 at the end).
 template <bool ISO>

@@ -32,6 +32,8 @@ def _f32(a) -> np.ndarray:
 
 # Storage forms of the wave fields (FLETCHER_FORM_*).
 FORMS = {"fp32": 0, "fp16": 1, "fp16x": 2}
+# Numerics of the FP32 step (FLETCHER_NUMERICS_*).
+NUMERICS = {"fast": 0, "d1d1": 1}
 
 
 class Propagator:
@@ -39,10 +41,12 @@ class Propagator:
 
     form: "fp32" (the reference's precision), "fp16" (FP16 fields with a
     power-of-two scale per z-plane) or "fp16x" (FP16 plus a residual byte per
-    value); the arithmetic is FP32 in every form."""
+    value); the arithmetic is FP32 in every form.
+    numerics: "fast" (default) or "d1d1" (the der1der1/ tree's operation
+    order, FP32 form only)."""
 
     def __init__(self, tile_rows: int = 0, stages: int = 0, zchunks: int = 0, stream: int | None = None,
-                 form: str = "fp32"):
+                 form: str = "fp32", numerics: str = "fast"):
         self.lib = _lib.load()
         self.lib.FLETCHER_ClearError()
         if stream is not None:
@@ -52,6 +56,10 @@ class Propagator:
         self.form = form
         if self.lib.FLETCHER_SetForm(FORMS[form]):
             _check(self.lib, "SetForm")
+        if numerics not in NUMERICS:
+            raise ValueError(f"unknown numerics {numerics!r}; one of {sorted(NUMERICS)}")
+        if self.lib.FLETCHER_SetNumerics(NUMERICS[numerics]):
+            _check(self.lib, "SetNumerics")
         if self.lib.FLETCHER_SetTileConfig(tile_rows, stages, zchunks):
             _check(self.lib, "SetTileConfig")
         self.shape = None

@@ -254,8 +254,7 @@ def run_boundary(kind: str, n: int, steps: int, snaps, seed: int = 1, stream=Non
     lib.FLETCHER_AbcSetInterval(1)
     prop.finalize()
     Propagator()  # back to the default tile shape
-    _, interval = _split_kind(kind)
-    extra = {"learned": 3 + 1.0 / interval, "oneway": 3, "sponge": 1}.get(base, 0)
+    extra = {"learned": 1, "oneway": 1, "sponge": 1}.get(base, 0)  # one boundary launch after the step
     extra += 1 if damping > 0 and base in ("learned", "oneway") else 0
     return out, ms / max(snaps), 1 + extra, (rows.value, stages.value)
 

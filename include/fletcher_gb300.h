@@ -26,7 +26,9 @@ extern "C" {
 /* Replaces original/driver.h:8-12.  Copies the six raw model arrays and the
  * four initial fields (sx*sy*sz floats each, x fastest) to the GPU, computes
  * the ten coefficient fields there in FP64 (original/precomp.h:14-58) and
- * keeps everything resident.  Requires bord >= 4 (the stencil radius). */
+ * keeps everything resident.  Requires bord >= 4 (the stencil radius).  A
+ * model value that is not finite (NaN or infinity) is rejected with
+ * FLETCHER_ERR_ARGS, naming the array and the cell. */
 void DRIVER_Initialize(const int sx, const int sy, const int sz, const int bord, float dx,
                        float dy, float dz, float dt, float *vpz, float *vsv, float *epsilon,
                        float *delta, float *phi, float *theta, float *pp, float *pc, float *qp,
@@ -104,6 +106,46 @@ int FLETCHER_HostAccess(void);
 #define FLETCHER_FORM_FP16 1
 #define FLETCHER_FORM_FP16X 2
 int FLETCHER_SetForm(int form);
+
+/* Numerics of the FP32 step, chosen before DRIVER_Initialize.  The
+ * reference ships each formulation as its own source tree; this selects
+ * between two of them in one library.
+ * FLETCHER_NUMERICS_FAST (default): the update of original/sample.h:32-89
+ *   with each DerCross evaluated as a first derivative of a first derivative
+ *   (equal in real arithmetic: its weights are products of the Der1
+ *   weights) and fused multiply-adds; within 1e-5 relative L2 of both trees
+ *   over short runs.
+ * FLETCHER_NUMERICS_D1D1: the Der1-Der1 tree's formulation and operation
+ *   order (der1der1/sample.h:35-120): first derivatives scaled and kept
+ *   (pDx = Der1_x(p)/dx, pDy = Der1_y(p)/dy), mixed derivatives as their
+ *   first derivatives (pxy = Der1_y(pDx)/dy, pxz = Der1_z(pDx)/dz,
+ *   pyz = Der1_z(pDy)/dz), every operation rounded on its own in the
+ *   reference's order -- the floats of that tree built without
+ *   floating-point contraction.  FP32 form, single shot, 16 x 4 tiles.
+ * Returns a FLETCHER_* status. */
+#define FLETCHER_NUMERICS_FAST 0
+#define FLETCHER_NUMERICS_D1D1 1
+int FLETCHER_SetNumerics(int mode);
+
+/* Fault injection for tests of the failure paths (no counterpart in the
+ * reference, whose back-ends exit on any error).  Nothing here faults or
+ * hangs the GPU.
+ * FLETCHER_FAULT_ALLOC: the device allocation `arg` allocations from now
+ *   (0 = the next one) fails as if memory were exhausted; the call that
+ *   makes it reports FLETCHER_ERR_NOMEM and releases what it allocated.
+ * FLETCHER_FAULT_STALL: in the next propagate launch (FP32 form, default
+ *   16 x 5 tiles and numerics; that launch uses a variant of the kernel
+ *   built with the hook, the regular kernels carry none), CTA 0
+ *   skips the loads of its step `arg` (counted from 0), and every wait of
+ *   that launch gives up after wait_us microseconds (1000 .. 2000000); the
+ *   CTA's waits for that stage run out, it drains the loads in flight and
+ *   leaves, and the step reports FLETCHER_ERR_TIMEOUT.  The fields of that
+ *   step are then undefined; the state stays usable (re-initialise it).
+ * FLETCHER_FAULT_NONE: cancels pending injections. */
+#define FLETCHER_FAULT_NONE 0
+#define FLETCHER_FAULT_ALLOC 1
+#define FLETCHER_FAULT_STALL 2
+int FLETCHER_InjectFault(int kind, int arg, int wait_us);
 
 /* Kernel shape override for tuning (0 keeps the default): rows per tile,
  * pipeline stages, z-chunks per column (> 0: that many, the last partial

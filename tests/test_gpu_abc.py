@@ -207,7 +207,7 @@ def test_training_and_reflected_energy_small():
     assert 0.0 < e["oneway"] < e["plain8"]
     assert 0.0 < e["learned"] < 0.8 * e["oneway"]
     assert e["learned"] < e["random"]
-    assert res["learned"]["launches_per_step"] == 5 and res["oneway"]["launches_per_step"] == 4
+    assert res["learned"]["launches_per_step"] == 2 and res["oneway"]["launches_per_step"] == 2
 
 
 def test_interval_reuses_the_coefficients():
