@@ -575,19 +575,22 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_abc_forward(const float *f
 
 // ---- the boundary step: one cooperative launch after the plain step -----------
 //
-// For the face pairs normal to z, then y, then x (a bounded grid-wide
-// barrier between them: a pass reads the next values the previous pass wrote
-// at edge cells), every warp takes groups of 4 consecutive rays (16 ghost
+// Two kernels, one launch per step: k_abc_boundary on the steps where the
+// learned form evaluates its network, k_abc_rays_coop on the other steps and
+// for the medium's fixed coefficients.  Both run the face pairs normal to z,
+// then y, then x, with a bounded grid-wide barrier between them (a pass
+// reads the next values the previous pass wrote at edge cells).
+//
+// k_abc_boundary: every warp takes groups of 4 consecutive rays (16 ghost
 // cells):
 //  1. lane 8 r + q loads point q (d = L-7+q) of ray r's outward normal line
-//     at t from the current field and, in the learned form, at t-1 from the
-//     line buffer the previous launch filled; it stores the t line for the
-//     next launch;
-//  2. learned form, on an evaluation step: the 16 cells' features and the
-//     network on the tensor cores (mma.sync m16n8k16), two lanes per cell
-//     building the t and t-1 stencils; k = sigmoid(y) stays in registers
-//     (it is written to the coefficient buffer only when later steps reuse
-//     it); otherwise k comes from that buffer;
+//     at t from the current field and at t-1 from the line buffer the
+//     previous launch filled; it stores the t line when the next step
+//     evaluates the network too;
+//  2. the 16 cells' features and the network on the tensor cores
+//     (mma.sync m16n8k16), two lanes per cell building the t and t-1
+//     stencils; k = sigmoid(y) stays in registers (it is written to the
+//     coefficient buffer only when later steps reuse it);
 //  3. lanes 4 r + j (j = 0..3: d = L-3+j) apply the box-scheme update
 //     next_g = cur_i + k (cur_g - next_i) outward along ray r, an inclusive
 //     scan of affine maps over the ray's 4 lanes.
@@ -605,6 +608,7 @@ struct BoundaryArgs {
   float2 *k;                // per ghost cell: (k_p, k_q), read unless the network runs, written when it is kept
   int eval;                 // the network runs at this step
   int keep;                 // store the network's k for the steps that reuse it
+  int save;                 // store the t lines (the next step evaluates the network)
   unsigned *bar;            // grid barrier: arrival count, generation
   unsigned *err;            // error word (bit 0: a bounded wait gave up)
   unsigned long long wait_ns;
@@ -645,14 +649,13 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks, ui
   return ok_s != 0;
 }
 
-template <bool NET>
 __global__ void __launch_bounds__(32 * kBoundaryWarps, 2) k_abc_boundary(const __grid_constant__ BoundaryArgs B) {
-  __shared__ __align__(16) __half Xs[NET ? kBoundaryWarps : 1][16 * kXs];
-  __shared__ float2 Ln[kBoundaryWarps][NET ? 2 : 1][4][8];  // [time: t, t-1][ray][point] (p, q)
+  __shared__ __align__(16) __half Xs[kBoundaryWarps][16 * kXs];
+  __shared__ float2 Ln[kBoundaryWarps][2][4][8];  // [time: t, t-1][ray][point] (p, q)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const Ghost &G = B.G;
   Frags F;
-  if (NET && B.eval) load_frags(B.net, F);
+  load_frags(B.net, F);
   const long wg = (long)blockIdx.x * kBoundaryWarps + warp, nw = (long)gridDim.x * kBoundaryWarps;
   for (int A = 2; A >= 0; --A) {
     const int fa = 2 * (2 - A);                       // the low face; fa + 1 is the high one
@@ -670,21 +673,19 @@ __global__ void __launch_bounds__(32 * kBoundaryWarps, 2) k_abc_boundary(const _
           const int idx0 = __float_as_int(B.med[ray * kGhostD].w);  // cell d = L-3 (point 4)
           const int step = ray < rmid ? -stride : stride;
           a = __ldcg(B.cur + idx0 + (q - kGhostD) * step);
-          if constexpr (NET) {
-            if (B.eval) b = __ldcg(B.line_in + ray * 8 + q);
-            __stcg(B.line_out + ray * 8 + q, a);
-          }
+          b = __ldcg(B.line_in + ray * 8 + q);
+          if (B.save) __stcg(B.line_out + ray * 8 + q, a);
         }
         Ln[warp][0][r][q] = a;
-        if constexpr (NET) Ln[warp][NET ? 1 : 0][r][q] = b;
+        Ln[warp][1][r][q] = b;
       }
       __syncwarp();
       // 2. the coefficient of update lane u = 4 r + j (cell 4 r + j of the group).
       const int u = lane & 15;
       const long cell = ray0 * kGhostD + u;
       const bool live = lane < 16 && ray0 + (u >> 2) < r1;
-      float2 kc = make_float2(0.f, 0.f);
-      if (NET && B.eval) {
+      float2 kc;
+      {
         // Features of cell c = lane / 2 (ray c / 4, d = L-3 + c % 4); the
         // lane pair builds the t (even lane) and t-1 (odd lane) stencils.
         const int c = lane >> 1, half_t = lane & 1, j = c & 3;
@@ -707,7 +708,7 @@ __global__ void __launch_bounds__(32 * kBoundaryWarps, 2) k_abc_boundary(const _
         // hold values near the FP32 underflow, whose reciprocal overflows).
         if (!(s > kMinScale)) s = 0.f;
         const float inv = s > 0.f ? 1.0f / s : 0.f;
-        __half *X = Xs[NET ? warp : 0];
+        __half *X = Xs[warp];
         __half *row = X + c * kXs + 18 * half_t;
 #pragma unroll
         for (int k = 0; k < 18; k += 2)
@@ -729,8 +730,6 @@ __global__ void __launch_bounds__(32 * kBoundaryWarps, 2) k_abc_boundary(const _
         const float b0 = __shfl_sync(0xffffffffu, yhi[0], src), b1 = __shfl_sync(0xffffffffu, yhi[1], src);
         kc = u < 8 ? make_float2(sigmoid(a0), sigmoid(a1)) : make_float2(sigmoid(b0), sigmoid(b1));
         if (B.keep && live) B.k[cell] = kc;
-      } else if (live) {
-        kc = B.k[cell];
       }
       // 3. the update along each ray (lanes 0 .. 15).
       const int r = u >> 2, j = u & 3;
@@ -766,6 +765,78 @@ __global__ void __launch_bounds__(32 * kBoundaryWarps, 2) k_abc_boundary(const _
       }
       if (live) __stcg(B.next + gidx, make_float2(ax, ay));
       __syncwarp();
+    }
+    if (A > 0 && !grid_barrier(B.bar, gridDim.x, B.wait_ns, B.err)) return;
+  }
+}
+
+// k_abc_rays_coop: the update with coefficients from the buffer (the
+// medium's, or the network's from its last evaluation), four lanes per ray
+// (j = 0..3: d = L-3+j), eight rays per warp.  Each lane loads its cell's
+// coefficient and value at t, the lane of d = L-3 also the inward
+// neighbour's values at t and t+1; the outward dependence is an inclusive
+// scan of affine maps over the ray's 4 lanes.  SAVE: the step before an
+// evaluation also stores the rays' 8 line points at t (lane j: points j
+// and j+4), which the evaluating step reads as its t-1 lines.
+template <bool SAVE>
+__global__ void __launch_bounds__(256) k_abc_rays_coop(const __grid_constant__ BoundaryArgs B) {
+  const Ghost &G = B.G;
+  const int lane = threadIdx.x & 31, j = lane & 3;
+  const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x, nth = (long)gridDim.x * blockDim.x;
+  for (int A = 2; A >= 0; --A) {
+    const int fa = 2 * (2 - A);
+    const long r0 = G.off[fa] / kGhostD, rmid = G.off[fa + 1] / kGhostD, r1 = G.off[fa + 2] / kGhostD;
+    const int stride = A == 0 ? 1 : (A == 1 ? B.pitch : B.sy * B.pitch);
+    const long total = ((r1 - r0) * kGhostD + 31) / 32 * 32;  // whole warps iterate together
+    for (long t = tid; t < total; t += nth) {
+      const long ray = r0 + (t >> 2);
+      const bool live = ray < r1;
+      const long cell = ray * kGhostD + j;
+      float2 kk = make_float2(0.f, 0.f), cg = kk, ci = kk, ni = kk, far = kk;
+      int gidx = 0, step = 0;
+      if (live) {
+        kk = B.k[cell];
+        gidx = __float_as_int(B.med[cell].w);
+        step = ray < rmid ? -stride : stride;
+        cg = __ldcg(B.cur + gidx);
+        if (SAVE) far = __ldcg(B.cur + gidx - kGhostD * step);  // line point j (d = L-7+j)
+        if (j == 0) {
+          if (!SAVE) ci = __ldcg(B.cur + gidx - step);
+          ni = __ldcg(B.next + gidx - step);  // next of d = L-4
+        }
+        if (SAVE) {
+          __stcg(B.line_out + ray * 8 + j, far);
+          __stcg(B.line_out + ray * 8 + kGhostD + j, cg);
+        }
+      }
+      // The inward cell of lanes 1 .. 3 is the cell of the lane before; that
+      // of lane 0 is line point 3, which lane 3 loaded when saving.
+      {
+        const float ux = __shfl_up_sync(0xffffffffu, cg.x, 1), uy = __shfl_up_sync(0xffffffffu, cg.y, 1);
+        const float fx = __shfl_sync(0xffffffffu, far.x, lane | 3), fy = __shfl_sync(0xffffffffu, far.y, lane | 3);
+        if (j != 0) ci = make_float2(ux, uy);
+        else if (SAVE) ci = make_float2(fx, fy);
+      }
+      float ax = __fmaf_rn(kk.x, cg.x, ci.x), ay = __fmaf_rn(kk.y, cg.y, ci.y);
+      float mx = -kk.x, my = -kk.y;
+      if (j == 0) {
+        ax = __fmaf_rn(mx, ni.x, ax);
+        ay = __fmaf_rn(my, ni.y, ay);
+        mx = 0.f;
+        my = 0.f;
+      }
+#pragma unroll
+      for (int o = 1; o < kGhostD; o <<= 1) {
+        const float px = __shfl_up_sync(0xffffffffu, ax, o), py = __shfl_up_sync(0xffffffffu, ay, o);
+        const float qx = __shfl_up_sync(0xffffffffu, mx, o), qy = __shfl_up_sync(0xffffffffu, my, o);
+        if (j >= o) {
+          ax = __fmaf_rn(mx, px, ax);
+          ay = __fmaf_rn(my, py, ay);
+          mx *= qx;
+          my *= qy;
+        }
+      }
+      if (live) __stcg(B.next + gidx, make_float2(ax, ay));
     }
     if (A > 0 && !grid_barrier(B.bar, gridDim.x, B.wait_ns, B.err)) return;
   }
@@ -1008,8 +1079,8 @@ struct ResidentLayer {
   float4 *med = nullptr;       // medium of every ghost cell (one-way modes)
   float2 *k = nullptr;         // one-way coefficients of every ghost cell (fixed, or the network's kept ones)
   float2 *lines[2] = {nullptr, nullptr};  // learned form: t-1 line points of every ray, by step parity
-  unsigned *bar = nullptr;     // the boundary kernel's grid barrier (count, generation)
-  int grid = 0;                // its cooperative grid
+  unsigned *bar = nullptr;     // the boundary kernels' grid barrier (count, generation)
+  int grid_net = 0, grid_rays = 0;  // their cooperative grids
   LayerCell *cells = nullptr;  // every layer cell (taper), z, y, x order
   long ncells = 0;
 };
@@ -1112,15 +1183,18 @@ cudaError_t abc_after_step(const ResidentView &v) {
     a.line_in = R.lines[R.steps & 1];
     a.line_out = R.lines[(R.steps + 1) & 1];
     a.k = R.k;
-    a.eval = learned && R.steps % R.interval == 0;  // the last coefficients stay in between
+    a.eval = learned && R.steps % R.interval == 0;        // the last coefficients stay in between
     a.keep = learned && R.interval > 1;
+    a.save = learned && (R.steps + 1) % R.interval == 0;  // the next step evaluates
     a.bar = R.bar;
     a.err = v.err;
     a.wait_ns = kWaitLimitNs;
     ++R.steps;
     void *args[] = {&a};
-    const void *kern = learned ? (const void *)k_abc_boundary<true> : (const void *)k_abc_boundary<false>;
-    const cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(R.grid), dim3(32 * kBoundaryWarps), args, 0, v.stream);
+    const void *kern = a.eval ? (const void *)k_abc_boundary
+                              : (a.save ? (const void *)k_abc_rays_coop<true> : (const void *)k_abc_rays_coop<false>);
+    const int grid = a.eval ? R.grid_net : R.grid_rays;
+    const cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(256), args, 0, v.stream);
     if (e != cudaSuccess) return e;
   }
   if (R.damping > 0.f && R.ncells)
@@ -1366,13 +1440,18 @@ extern "C" int FLETCHER_SetBoundary(int mode, int layer, float damping) {
     }
     CKA(cudaMalloc(&R.bar, 2 * sizeof(unsigned)));
     CKA(cudaMemsetAsync(R.bar, 0, 2 * sizeof(unsigned), v.stream));
-    // Cooperative grid: every block resident at once (the grid barrier needs it).
+    // Cooperative grids: every block resident at once (the grid barrier needs it).
+    const int sms = v.num_sms > 0 ? v.num_sms : 1;
     int per_sm = 0;
-    const void *kern = mode == FLETCHER_BOUNDARY_LEARNED ? (const void *)k_abc_boundary<true>
-                                                         : (const void *)k_abc_boundary<false>;
-    CKA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kBoundaryWarps, 0));
+    CKA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_abc_boundary, 256, 0));
     if (per_sm < 1) return err(FLETCHER_ERR_CUDA, "SetBoundary: the boundary kernel fits no block on an SM");
-    R.grid = per_sm * (v.num_sms > 0 ? v.num_sms : 1);
+    R.grid_net = per_sm * sms;
+    int per_sm_r = 0, per_sm_s = 0;
+    CKA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_r, k_abc_rays_coop<false>, 256, 0));
+    CKA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_s, k_abc_rays_coop<true>, 256, 0));
+    per_sm_r = std::min(std::min(per_sm_r, per_sm_s), 4);
+    if (per_sm_r < 1) return err(FLETCHER_ERR_CUDA, "SetBoundary: the ray kernel fits no block on an SM");
+    R.grid_rays = per_sm_r * sms;
   }
   if (damping > 0.f) {
     // Layer cells in z, y, x order (coalesced).

@@ -1296,7 +1296,15 @@ struct Batch {
   int sealed_rows = 0;
   ShotDesc *d_desc = nullptr;
   ShotMaps *d_maps = nullptr;
-  int4 *d_items = nullptr;
+  int4 *d_items = nullptr;          // 16-bit forms: {shot, x0, y0, chunk} items
+  // FP32: for r running shots (the first r of `order`), their single-shot
+  // plans stacked per CTA at d_plan + plan_off[r-1] ({x0 + (shot << 16), y0,
+  // z0, z1}), each CTA's first segment at d_first + (r-1) * (plan_ctas + 1).
+  int4 *d_plan = nullptr;
+  int *d_first = nullptr;
+  std::vector<long> plan_off;
+  std::vector<int> plan_grid;
+  int plan_ctas = 0;
   HalfShot *d_hshots = nullptr;     // 16-bit forms
   HalfShotMaps *d_hmaps = nullptr;
   int *d_order = nullptr;
@@ -1313,6 +1321,11 @@ struct Batch {
 Batch B;
 
 void batch_free_tables() {
+  if (B.d_plan) cudaFree(B.d_plan);
+  if (B.d_first) cudaFree(B.d_first);
+  B.d_plan = nullptr;
+  B.d_first = nullptr;
+  B.plan_ctas = 0;
   if (B.d_desc) cudaFree(B.d_desc);
   if (B.d_maps) cudaFree(B.d_maps);
   if (B.d_items) cudaFree(B.d_items);
@@ -1425,6 +1438,59 @@ int batch_seal(int rows, int stages) {
   return FLETCHER_OK;
 }
 
+// The FP32 batch's work split for `ctas` persistent CTAs: each shot's own
+// single-shot plan (plan_segments, the balanced split the shot would get
+// alone), and for every number r of running shots those of the first r
+// shots of `order` stacked per CTA -- CTA b runs its segments of
+// order[0], then of order[1], ...  So neighbouring CTAs work on
+// neighbouring tiles of the same shot, and every CTA's load is balanced
+// shot by shot.
+int batch_plan(int ctas) {
+  if (B.d_plan && B.plan_ctas == ctas) return FLETCHER_OK;
+  if (B.d_plan) cudaFree(B.d_plan);
+  if (B.d_first) cudaFree(B.d_first);
+  B.d_plan = nullptr;
+  B.d_first = nullptr;
+  const int ns = (int)B.shots.size();
+  if (ns >= 32768) return fail(FLETCHER_ERR_ARGS, "a batch holds at most 32767 shots");
+  std::vector<Split> per(ns);
+  for (int oi = 0; oi < ns; ++oi) {
+    const BatchShot &s = B.shots[B.order[oi]];
+    if (s.sx >= 65536) return fail(FLETCHER_ERR_ARGS, "batched shots need sx < 65536");
+    per[oi] = plan_segments(ctas, s.ntx, s.nty, B.sealed_rows, B.bord, s.sz - 2 * B.bord, 0);
+  }
+  std::vector<int4> plan;
+  std::vector<int> first((size_t)ns * (ctas + 1));
+  B.plan_off.assign(ns, 0);
+  B.plan_grid.assign(ns, 1);
+  for (int r = 1; r <= ns; ++r) {
+    const size_t base = plan.size();
+    B.plan_off[r - 1] = (long)base;
+    int *f = first.data() + (size_t)(r - 1) * (ctas + 1);
+    for (int b = 0; b < ctas; ++b) {
+      f[b] = (int)(plan.size() - base);
+      for (int oi = 0; oi < r; ++oi) {
+        const Split &sp = per[oi];
+        const int shot = B.order[oi];
+        for (int k = sp.first[b]; k < sp.first[b + 1]; ++k) {
+          const int4 w = sp.seg[k];
+          plan.push_back(make_int4(w.x | (shot << 16), w.y, w.z, w.w));
+        }
+      }
+    }
+    f[ctas] = (int)(plan.size() - base);
+    int grid = ctas;  // CTAs past the last one with work are not launched
+    while (grid > 1 && f[grid - 1] == f[grid]) --grid;
+    B.plan_grid[r - 1] = grid;
+  }
+  CK(dev_malloc(&B.d_plan, sizeof(int4) * plan.size()));
+  CK(dev_malloc(&B.d_first, sizeof(int) * first.size()));
+  CK(cudaMemcpy(B.d_plan, plan.data(), sizeof(int4) * plan.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(B.d_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice));
+  B.plan_ctas = ctas;
+  return FLETCHER_OK;
+}
+
 int batch_max_steps() {
   int m = 0;
   for (auto &s : B.shots) m = std::max(m, s.nsteps);
@@ -1488,6 +1554,9 @@ int batch_issue(int it0, int it1, const float *src) {
       B.launches += 2;
       continue;
     }
+    P.seg = B.d_plan + B.plan_off[active - 1];
+    P.cta_first = B.d_first + (size_t)(active - 1) * (B.plan_ctas + 1);
+    L.grid = B.plan_grid[active - 1];
     CK(propagate_fp32_launch(L, g_stream));
     ++B.launches;
   }
@@ -1650,6 +1719,7 @@ extern "C" int FLETCHER_BatchRun(const float *src, int max_steps, int use_graph,
   if (per_sm < 1)
     return fail(FLETCHER_ERR_CUDA, "tile shape (%d rows, %d stages) fits no CTA on an SM", B.sealed_rows, B.stages);
   B.ctas = B.num_sms * per_sm;
+  if (!batch_half() && batch_plan(B.ctas)) return g_last_err;
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));

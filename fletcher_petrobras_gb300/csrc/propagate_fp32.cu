@@ -79,7 +79,9 @@ struct Item {
 // Work-item kinds of a launch (template parameter MODE):
 //  * kItemsTiles: single shot, items = tiles x uniform z-chunks, chunk-major,
 //    CTA b takes b, b + grid, ... (decoded arithmetically, no lookups);
-//  * kItemsBatch: batched shots, P.items {shot, x0, y0, chunk}, same order;
+//  * kItemsBatch: batched shots, P.seg {x0 + (shot << 16), y0, z0, z1}, CTA
+//    b takes its run cta_first[b] .. cta_first[b + 1] - 1 (each running
+//    shot's own single-shot plan, stacked);
 //  * kItemsSegments: single shot, P.seg {x0, y0, z0, z1}, CTA b takes its run
 //    cta_first[b] .. cta_first[b + 1] - 1.
 constexpr int kItemsTiles = 0, kItemsBatch = 1, kItemsSegments = 2;
@@ -88,13 +90,12 @@ template <int TY, int MODE>
 __device__ __forceinline__ Item decode_item(int item, const PropParams &P) {
   Item it;
   if constexpr (MODE == kItemsBatch) {
-    const int4 w = P.items[item];  // {shot, x0, y0, chunk index}
-    const ShotDesc &d = P.shots[w.x];
-    it.x0 = w.y;
-    it.y0 = w.z;
-    it.z0 = d.bord + w.w * d.chunk;
-    it.z1 = min(it.z0 + d.chunk, d.sz - d.bord);
-    it.shot = w.x;
+    const int4 w = P.seg[item];  // {x0 + (shot << 16), y0, z0, z1}
+    it.x0 = w.x & 0xffff;
+    it.y0 = w.y;
+    it.z0 = w.z;
+    it.z1 = w.w;
+    it.shot = w.x >> 16;
   } else if constexpr (MODE == kItemsSegments) {
     const int4 w = P.seg[item];  // {x0, y0, z0, z1}
     it.x0 = w.x;
@@ -123,7 +124,7 @@ struct ItemRange {
 };
 template <int MODE>
 __device__ __forceinline__ ItemRange item_range(const PropParams &P) {
-  if constexpr (MODE == kItemsSegments) return {P.cta_first[blockIdx.x], P.cta_first[blockIdx.x + 1], 1};
+  if constexpr (MODE != kItemsTiles) return {P.cta_first[blockIdx.x], P.cta_first[blockIdx.x + 1], 1};
   else return {(int)blockIdx.x, P.nitems, (int)gridDim.x};
 }
 
@@ -137,7 +138,6 @@ struct StepMaps {
 struct Cursor {
   Item it;
   int item, k, stage;
-  int n;  // steps issued so far by this CTA
 };
 
 // Issues the TMA loads of one step (plane k of item `it`) into `stage`.
@@ -186,8 +186,9 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   const ItemRange R = item_range<MODE>(P);
   if (R.first >= R.end) return;
   volatile int *s_end = s_abort + 1;
-  auto item_end = [&]() { return MODE == kItemsSegments ? *s_end : P.nitems; };
-  auto item_step = [&]() { return MODE == kItemsSegments ? 1 : (int)gridDim.x; };
+  int *s_issued = s_abort + 2;  // fault-injection variant: steps this CTA has issued
+  auto item_end = [&]() { return MODE != kItemsTiles ? *s_end : P.nitems; };
+  auto item_step = [&]() { return MODE != kItemsTiles ? 1 : (int)gridDim.x; };
   // The producer is lane 0 of the last warp (warps 0 .. TY/4-1 carry the
   // halo-column work).  Its cursor, in shared memory, is the next step to load.
   const bool producer = tid == (TY - 1) * 32;
@@ -213,15 +214,31 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   // waits for that stage give up and the launch reports a timeout.)
   auto produce = [&]() {
     Cursor c = *cur;
-    if (!HOOK || c.n != P.stall_step || blockIdx.x != 0)
+    if constexpr (HOOK) {
+      if (*s_issued != P.stall_step || blockIdx.x != 0)
+        issue_step<TY>(smem + c.stage * G::STAGE_B, &full[c.stage], c.it, c.k, maps_of(c.it));
+      ++*s_issued;
+    } else {
       issue_step<TY>(smem + c.stage * G::STAGE_B, &full[c.stage], c.it, c.k, maps_of(c.it));
-    if constexpr (HOOK) ++c.n;
+    }
     if (++c.stage == S) c.stage = 0;
     if (++c.k >= c.it.z1 + kRadius) {
       c.item += item_step();
       if (c.item < item_end()) {
         c.it = decode_item<TY, MODE>(c.item, P);
         c.k = c.it.z0 - kRadius;
+        if constexpr (BATCH) {
+          // Batched shots keep their tensor maps in global memory: fetch
+          // those of the item after this one into the descriptor cache now,
+          // an item ahead of their first use.
+          if (c.item + 1 < item_end()) {
+            const StepMaps m = maps_of(decode_item<TY, MODE>(c.item + 1, P));
+            tma_prefetch_desc(m.cur);
+            tma_prefetch_desc(m.prev);
+            tma_prefetch_desc(m.arr);
+            tma_prefetch_desc(m.upd);
+          }
+        }
       }
     }
     *cur = c;
@@ -231,7 +248,8 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
     mbar_init(xchg, TY);
     mbar_fence_init();
     *s_abort = 0;
-    if constexpr (MODE == kItemsSegments) *s_end = R.end;
+    *s_issued = 0;
+    if constexpr (MODE != kItemsTiles) *s_end = R.end;
   }
   if (producer) {
     Cursor c;
@@ -239,7 +257,6 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
     c.item = R.first;
     c.k = c.it.z0 - kRadius;
     c.stage = 0;
-    c.n = 0;
     *cur = c;
   }
   __syncthreads();
@@ -250,6 +267,13 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
       tma_prefetch_desc(m.prev);
       tma_prefetch_desc(m.arr);
       tma_prefetch_desc(m.upd);
+      if (BATCH && cur->item + 1 < item_end()) {
+        const StepMaps m2 = maps_of(decode_item<TY, MODE>(cur->item + 1, P));
+        tma_prefetch_desc(m2.cur);
+        tma_prefetch_desc(m2.prev);
+        tma_prefetch_desc(m2.arr);
+        tma_prefetch_desc(m2.upd);
+      }
     }
     // Prologue: the first S-2 steps of this CTA.
     for (int a = 0; a < S - 2 && cur->item < item_end(); ++a) produce();

@@ -127,6 +127,20 @@ struct HItem {
   int x0, y0, z0, z1;
 };
 
+// Fetches a step's tensor maps into the descriptor cache (the residual
+// maps exist in the extended form only).
+template <bool EXT>
+__device__ __forceinline__ void prefetch_maps(const HalfMaps &m) {
+  tma_prefetch_desc(&m.cur_hi);
+  tma_prefetch_desc(&m.prev_hi);
+  if constexpr (EXT) {
+    tma_prefetch_desc(&m.cur_lo);
+    tma_prefetch_desc(&m.prev_lo);
+  }
+  tma_prefetch_desc(&m.arr);
+  tma_prefetch_desc(&m.upd);
+}
+
 // Segment `item` of the launch's list: {x0, y0, z0, z1}.
 __device__ __forceinline__ HItem decode_hitem(int item, const PropParams &P) {
   const int4 w = P.seg[item];
@@ -528,7 +542,12 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
     if (++stg == S) stg = 0;
     if (++k >= it.z1 + kRadius) {
       item += item_step();
-      if (item < item_end()) k = decode_bitem(item, P).z0 - kRadius;
+      if (item < item_end()) {
+        k = decode_bitem(item, P).z0 - kRadius;
+        // The shots' tensor maps live in global memory: fetch those of the
+        // item after this one into the descriptor cache, an item ahead.
+        if (item + item_step() < item_end()) prefetch_maps<EXT>(maps_of(decode_bitem(item + item_step(), P)));
+      }
     }
     cur[0] = item;
     cur[1] = k;
@@ -548,6 +567,8 @@ __global__ void __launch_bounds__(kTileX *TY, 1)
   }
   __syncthreads();
   if (producer) {
+    prefetch_maps<EXT>(maps_of(decode_bitem(item_first, P)));
+    if (item_first + item_step() < item_end()) prefetch_maps<EXT>(maps_of(decode_bitem(item_first + item_step(), P)));
     // Prologue: S-1 steps; afterwards each step refills the stage freed by
     // the step before it.
     for (int a = 0; a < S - 1 && cur[0] < item_end(); ++a) produce();

@@ -282,3 +282,35 @@ def compare(n: int = 256, steps: int = 1500, nsnap: int = 5, kinds=("random", "l
                   "launches_per_step": launches, "tile": list(shape)}
     res["snapshots"] = snaps
     return res
+
+
+def profile_case(kind: str = "learned", n: int = 256, steps: int = 24, seed: int = 0) -> float:
+    """A short run of one boundary form with the network's initial weights
+    (untrained: the kernels' work does not depend on the weights) and the
+    default tile shape: the case the boundary kernels are profiled on.
+    Returns (and prints) the device ms per step.
+
+        python -c "from fletcher_petrobras_gb300 import learned; learned.profile_case('learned@8', 256, 24)"
+    """
+    import torch
+
+    init(seed)
+    base, _ = _split_kind(kind)
+    prob = boundary_problem(base, n, steps, seed)
+    model = prob.model() if base == "random" else prob.raw_model()
+    st = torch.cuda.Stream()
+    prop = Propagator(stream=st.cuda_stream)
+    prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model)
+    _set_boundary(prop.lib, kind, 0.0)
+    src = prob.sources(steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    prop.run(steps, prob.i_source, src)
+    e1.record(st)
+    prop.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    prop.lib.FLETCHER_SetBoundary(BOUNDARY_PLAIN, 0, 0.0)
+    prop.lib.FLETCHER_AbcSetInterval(1)
+    prop.finalize()
+    print(f"{kind} {n}^3: {ms:.4f} ms per step")
+    return ms

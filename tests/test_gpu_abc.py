@@ -255,3 +255,69 @@ def test_collection_and_training_are_reproducible():
     assert len(runs[0][0]) > 100
     for a, b in zip(runs[0], runs[1]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("interval", [1, 2])
+def test_fused_boundary_rollout_vs_cpu_oracle(interval, orc):
+    """Four steps of the learned layer (one boundary launch per step: the
+    network kernel on evaluation steps, the ray kernel in between) against
+    a CPU rollout: the oracle's plain step, its features of (t, t-1) --
+    after the first step the GPU takes t-1 from the line buffer it carried
+    over, not from the field -- its network and its box-scheme update.  The
+    network's k is held for `interval` steps."""
+    from oracle import abc_mlp
+
+    learned.init(6)
+    P = learned.get_weights()
+    prob = learned.boundary_problem("learned", 16, 150)
+    model = prob.raw_model()
+    prop = Propagator()
+    prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model)
+    prop.run(150, prob.i_source, prob.sources(150))
+    prop.synchronize()
+    f = [prop.field(k) for k in (2, 0, 3, 1)]  # pp pc qp qc
+    coef = prop.coefficients()
+    prop.finalize()
+    steps = 4
+    prop = Propagator()
+    prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model, *f)
+    assert prop.lib.FLETCHER_AbcSetInterval(interval) == 0
+    assert prop.lib.FLETCHER_SetBoundary(learned.BOUNDARY_LEARNED, learned.LAYER, 0.0) == 0
+    prop.run(steps)
+    prop.synchronize()
+    got = np.stack([prop.field(0), prop.field(1)])
+    prop.lib.FLETCHER_SetBoundary(learned.BOUNDARY_PLAIN, 0, 0.0)
+    prop.lib.FLETCHER_AbcSetInterval(1)
+    prop.finalize()
+    # CPU rollout.  The oracle's time loop always adds a source; it is put at
+    # grid cell 0, which no update reads, and that cell is left out below.
+    shape = (prob.sz, prob.sy, prob.sx)
+    quiet = prob.with_(source=(0, 0, 0))
+    b, L = prob.bord, learned.LAYER
+    lo, hi = (b + L,) * 3, (prob.sx - b - L, prob.sy - b - L, prob.sz - b - L)
+    cells = abc_mlp.ghost_cells(lo, hi, L)
+    c4 = coef.reshape((10,) + shape)
+    h = (prob.dx, prob.dy, prob.dz)
+    prev = np.stack([f[0], f[2]]).astype(np.float32)
+    cur = np.stack([f[1], f[3]]).astype(np.float32)
+    k = None
+    size = 0.0
+    for s in range(steps):
+        p1, q1, _, _ = orc.run_f32(quiet, model, steps=1, coef=coef, fields=(prev[0], cur[0], prev[1], cur[1]))
+        base = np.stack([p1, q1]).reshape((2,) + shape).astype(np.float64)
+        c64 = cur.reshape((2,) + shape).astype(np.float64)
+        if s % interval == 0:
+            X, _ = abc_mlp.features_targets(c64, prev.reshape((2,) + shape).astype(np.float64), c4, lo, hi, L, cells,
+                                            h, prob.dt, targets=False)
+            y, _ = abc_mlp.forward(P, X)
+            k = abc_mlp.sigmoid(y)
+        new = abc_mlp.oneway_update(c64, base.copy(), lo, hi, L, k)
+        size = max(size, float(np.max(np.abs(new - base))))
+        prev, cur = cur, new.reshape(2, -1).astype(np.float32)
+    want = cur.reshape(2, -1).astype(np.float64)
+    g = got.astype(np.float64)
+    g[:, 0] = want[:, 0] = 0.0
+    assert size > 0
+    err = float(np.max(np.abs(g - want)))
+    print(f"interval {interval}: max |GPU - oracle| {err:.3g} against an update size {size:.3g}")
+    assert err < 3e-2 * size + 1e-6 * np.abs(want).max()
