@@ -437,8 +437,9 @@ int FLETCHER_AbcForward(const float *features, int n, float *out);
 /* Boundary of the resident FP32 state, a layer of `layer` cells (>= 5)
  * inside the updated region (interior = updated region shrunk by `layer`).
  * FLETCHER_BOUNDARY_PLAIN: none.  FLETCHER_BOUNDARY_ONEWAY and
- * FLETCHER_BOUNDARY_LEARNED: the ghost-zone update after every step (three
- * launches; the learned form adds one inference launch before the step).
+ * FLETCHER_BOUNDARY_LEARNED: the ghost-zone update after every step, in one
+ * cooperative launch that also evaluates the network on the learned form's
+ * evaluation steps (two launches per step in all).
  * damping > 0 also scales every layer cell by exp(-(damping d)^2) after the
  * step; FLETCHER_BOUNDARY_SPONGE is that scaling alone (damping > 0).
  * FLETCHER_AbcLayerCells: ghost cells updated per step (one-way forms). */
