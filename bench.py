@@ -284,6 +284,35 @@ def run_gb300(args, ws, rank, local, group):
     peak, peak_kind = measured_peak()
     tpc = ncu_traffic_per_cell() if form == "fp32" else None
 
+    # End to end through the C ABI with host buffers (the reference's Model() sequence).
+    import ctypes as C
+
+    stats = (C.c_double * 5)()
+    e2e = e2e_wall = parity = e2e_clk = None
+    KE = args.e2e_steps or prob.steps  # the workload's own step count (1000 at C1)
+    if not args.no_e2e:
+        f = np.zeros((4, prob.n), np.float32)
+        from fletcher_petrobras_gb300.driver import FORMS
+
+        lib.FLETCHER_SetForm(FORMS[form])
+        lib.FLETCHER_SetStream(None)  # the library's own stream, as a plain C caller has it
+        group.barrier()
+        e2e_clocks = ClockSampler(local)
+        e2e_clocks.start()
+        rc = lib.FLETCHER_Model(KE, prob.i_source, prob.fcut, 0.01, prob.sx, prob.sy, prob.sz, prob.bord, prob.dx,
+                                prob.dy, prob.dz, prob.dt, *[fptr(f[k]) for k in range(4)],
+                                *[fptr(model[k]) for k in range(6)], stats)
+        e2e_clk = e2e_clocks.stop()
+        if rc:
+            raise RuntimeError("FLETCHER_Model failed: " + lib.FLETCHER_GetLastErrorString().decode())
+        lib.FLETCHER_SetForm(FORMS["fp32"])
+        phases = (C.c_double * 4)()
+        lib.FLETCHER_ModelPhases(phases)
+        e2e_wall = group.reduce(stats[2], "max")
+        e2e = ws * cells * KE / e2e_wall / 1e6
+        parity = reference_parity(prob, KE, form, f[1], f[3])  # FLETCHER_Model leaves the final p, q in pc, qc
+        del f
+
     # The other storage forms on the same workload (fewer steps).
     forms = {}
     if not args.no_forms:
@@ -298,31 +327,6 @@ def run_gb300(args, ws, rank, local, group):
                         "hbm_gbs": round(fbpc * cells / (fms / 1e3 / fk) / 1e9, 1)}
         for f in forms:
             forms[f]["speedup_vs_this_form"] = round((ms_max / K) / forms[f]["ms_per_step"], 3)
-
-    # End to end through the C ABI with host buffers (the reference's Model() sequence).
-    import ctypes as C
-
-    stats = (C.c_double * 5)()
-    e2e = e2e_wall = parity = None
-    KE = args.e2e_steps or prob.steps  # the workload's own step count (1000 at C1)
-    if not args.no_e2e:
-        f = np.zeros((4, prob.n), np.float32)
-        from fletcher_petrobras_gb300.driver import FORMS
-
-        lib.FLETCHER_SetForm(FORMS[form])
-        group.barrier()
-        rc = lib.FLETCHER_Model(KE, prob.i_source, prob.fcut, 0.01, prob.sx, prob.sy, prob.sz, prob.bord, prob.dx,
-                                prob.dy, prob.dz, prob.dt, *[fptr(f[k]) for k in range(4)],
-                                *[fptr(model[k]) for k in range(6)], stats)
-        if rc:
-            raise RuntimeError("FLETCHER_Model failed: " + lib.FLETCHER_GetLastErrorString().decode())
-        lib.FLETCHER_SetForm(FORMS["fp32"])
-        phases = (C.c_double * 4)()
-        lib.FLETCHER_ModelPhases(phases)
-        e2e_wall = group.reduce(stats[2], "max")
-        e2e = ws * cells * KE / e2e_wall / 1e6
-        parity = reference_parity(prob, KE, form, f[1], f[3])  # FLETCHER_Model leaves the final p, q in pc, qc
-        del f
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -361,6 +365,7 @@ def run_gb300(args, ws, rank, local, group):
                 "d2h_bytes_per_step": int(stats[4] / KE), "wall_s": round(e2e_wall, 3), "steps": KE,
                 "phases_s": {"setup": round(phases[0], 3), "steps": round(phases[1], 3),
                              "snapshot_drain": round(phases[2], 3), "readback_finalize": round(phases[3], 3)},
+                "clocks": e2e_clk,
                 "what": f"FLETCHER_Model via the C ABI, the workload's {KE} steps: DRIVER_Initialize (H2D of 6 "
                         "model + 4 field arrays, FP64 coefficient precompute) + per step (InsertSource, Propagate) "
                         "+ D2H snapshot of p every 0.01 s simulated + final D2H of p,q"},
