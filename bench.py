@@ -257,7 +257,7 @@ def cpu_baseline_leg(prob, model, args):
 
     t = oracle.time_slab(prob, model, nplanes=16, min_seconds=args.cpu_seconds)
     return {"value": round(t["msamples"], 2), "unit": UNIT, "cores": t["threads"], "kind": "port",
-            "sample": f"{t['steps']} FP32 steps of a {t['planes']}-plane slab of the 576^3 grid "
+            "sample": f"{t['steps']} FP32 steps of a {t['planes']}-plane slab of the {prob.sx}^3 grid "
                       f"({t['cells']} updated cells/step, {t['seconds']:.1f} s), oracle restatement of "
                       "original/OpenMP/openmp_propagate.c + original/sample.h (reference build absent)"}
 
@@ -547,9 +547,8 @@ def run_reference(args, ws, rank, group):
     if rank != 0:
         return
     import oracle
-    from fletcher_petrobras_gb300.models import C1
 
-    prob = C1
+    prob = workload(args)  # C1, or the same generator at another interior size
     K, W = args.steps, args.warmup
     k_run, w_run = min(K, REF_MAX_STEPS), min(W, REF_MAX_WARMUP)
     r = reference_cpu(prob, k_run, w_run)
@@ -565,7 +564,7 @@ def run_reference(args, ws, rank, group):
             cpu["ftz"] = {"value": round(ftz["msamples"], 2), "steps": ftz["steps"] - ftz["warmup"],
                           "build": ftz["build"]}
         ms = 1e3 * r["timed_s"] / k_run
-        workload = (f"C1: plain FP32 single shot, {prob.nx}^3 interior ({prob.sx}^3 grid), bord 4, absorb 32, "
+        desc = (f"C1: plain FP32 single shot, {prob.nx}^3 interior ({prob.sx}^3 grid), bord 4, absorb 32, "
                     f"dt 0.6 ms, 8-layer seeded TTI, 15 Hz Ricker at {prob.src_xyz}; the reference's OpenMP "
                     "back-end in its Model() loop")
         steps_line = k_run
@@ -576,21 +575,33 @@ def run_reference(args, ws, rank, group):
         t = oracle.time_slab(prob, model, nplanes=16, steps=K)
         v = round(t["msamples"], 2)
         cpu = {"value": v, "unit": UNIT, "cores": t["threads"], "kind": "port",
-               "sample": f"{K} steps of a {t['planes']}-plane slab of the 576^3 grid (reference build absent)"}
+               "sample": f"{K} steps of a {t['planes']}-plane slab of the {prob.sx}^3 grid (reference build absent)"}
         ms = 1e3 * t["seconds"] / K
-        workload = ("C1: plain FP32 single shot, 504^3 interior (576^3 grid); each step is one propagation of a "
+        desc = (f"C1: plain FP32 single shot, {prob.nx}^3 interior ({prob.sx}^3 grid); each step is one propagation of a "
                     f"{t['planes']}-plane slab ({t['cells']} cells)")
         steps_line = K
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": steps_line,
         "warmup": w_run if r is not None else W, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded 8-layer TTI model)",
-        "config": {"workload": workload, "grid": [prob.sx, prob.sy, prob.sz],
+        "config": {"workload": desc, "grid": [prob.sx, prob.sy, prob.sz],
                    "updated_cells_per_step": prob.updated_cells},
         "cpu_baseline": cpu,
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "libraries_loaded": repo_libraries_loaded(),
     }
     print(json.dumps(line), flush=True)
+
+
+def repo_libraries_loaded():
+    """Shared libraries of this repository mapped into this process (the
+    reference arm must show none of the product's)."""
+    try:
+        with open("/proc/self/maps") as f:
+            paths = {ln.split()[-1] for ln in f if ln.rstrip().endswith(".so") and ROOT in ln}
+    except OSError:
+        return None
+    return sorted(os.path.relpath(p, ROOT) for p in paths)
 
 
 def main():
