@@ -99,13 +99,14 @@ def measured_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def ncu_traffic_per_cell():
-    """DRAM bytes per updated cell of the propagate kernel from the committed
-    ncu summary (profiles/propagate_fp32_traffic.json), or None."""
+def ncu_traffic_per_cell(layout):
+    """DRAM bytes per updated cell of the propagate kernel in this
+    coefficient layout from the committed ncu summary
+    (profiles/propagate_fp32_traffic.json), or None."""
     path = os.path.join(ROOT, "profiles", "propagate_fp32_traffic.json")
     try:
         with open(path) as f:
-            return float(json.load(f)["dram_bytes_per_cell"])
+            return float(json.load(f)[layout]["dram_bytes_per_cell"])
     except Exception:
         return None
 
@@ -181,17 +182,19 @@ LAUNCHES_PER_STEP = {"fp32": 1, "fp16": 2, "fp16x": 2}
 KERNEL = {"fp32": "k_propagate_fp32", "fp16": "k_propagate_half<EXT=false>", "fp16x": "k_propagate_half<EXT=true>"}
 
 
-def timed_run(prob, model, form, K, W, group, clocks=None):
+def timed_run(prob, model, form, K, W, group, clocks=None, layout="planes"):
     """W untimed steps, then K steps timed with CUDA events on the library's
-    stream.  Returns (ms, kernel launches, bytes per cell, device GB)."""
+    stream.  Returns (ms, kernel launches, bytes per cell, device GB, clocks,
+    coefficient layout)."""
     import torch
 
     from fletcher_petrobras_gb300 import Propagator
 
     src = prob.sources(W + K)
     stream = torch.cuda.Stream()
-    prop = Propagator(stream=stream.cuda_stream, form=form)
+    prop = Propagator(stream=stream.cuda_stream, form=form, coef_layout=layout)
     prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, model)
+    used_layout = prop.coef_layout()
     prop.run(W, prob.i_source, src[:W])
     prop.synchronize()
     launches0 = prop.kernel_launches()
@@ -213,7 +216,7 @@ def timed_run(prob, model, form, K, W, group, clocks=None):
     dev_gb = prop.device_bytes() / 1e9
     prop.finalize()
     Propagator(form="fp32")
-    return ms, launches, bpc, dev_gb, clk
+    return ms, launches, bpc, dev_gb, clk, used_layout
 
 
 def reference_parity(prob, steps, form, p, q):
@@ -274,7 +277,8 @@ def run_gb300(args, ws, rank, local, group):
     K, W = args.steps, args.warmup
     model = prob.model()
     form = args.form
-    ms, launches, bpc, dev_gb, clk = timed_run(prob, model, form, K, W, group, ClockSampler(local))
+    ms, launches, bpc, dev_gb, clk, layout = timed_run(prob, model, form, K, W, group, ClockSampler(local),
+                                                      layout=args.coef_layout)
 
     ms_max = group.reduce(ms, "max")
     cells = prob.updated_cells
@@ -282,7 +286,7 @@ def run_gb300(args, ws, rank, local, group):
     per_launch_s = ms / 1e3 / K
     achieved = bpc * cells / per_launch_s / 1e9
     peak, peak_kind = measured_peak()
-    tpc = ncu_traffic_per_cell() if form == "fp32" else None
+    tpc = ncu_traffic_per_cell(layout) if form == "fp32" else None
 
     # End to end through the C ABI with host buffers (the reference's Model() sequence).
     import ctypes as C
@@ -294,7 +298,10 @@ def run_gb300(args, ws, rank, local, group):
         f = np.zeros((4, prob.n), np.float32)
         from fletcher_petrobras_gb300.driver import FORMS
 
+        from fletcher_petrobras_gb300.driver import COEF_LAYOUTS
+
         lib.FLETCHER_SetForm(FORMS[form])
+        lib.FLETCHER_SetCoefLayout(COEF_LAYOUTS[args.coef_layout])
         lib.FLETCHER_SetStream(None)  # the library's own stream, as a plain C caller has it
         group.barrier()
         e2e_clocks = ClockSampler(local)
@@ -306,6 +313,7 @@ def run_gb300(args, ws, rank, local, group):
         if rc:
             raise RuntimeError("FLETCHER_Model failed: " + lib.FLETCHER_GetLastErrorString().decode())
         lib.FLETCHER_SetForm(FORMS["fp32"])
+        lib.FLETCHER_SetCoefLayout(COEF_LAYOUTS["planes"])
         phases = (C.c_double * 4)()
         lib.FLETCHER_ModelPhases(phases)
         e2e_wall = group.reduce(stats[2], "max")
@@ -316,17 +324,24 @@ def run_gb300(args, ws, rank, local, group):
     # The other storage forms on the same workload (fewer steps).
     forms = {}
     if not args.no_forms:
-        for f in ("fp32", "fp16x", "fp16"):
-            if f == form:
+        # The FP32 form in the other coefficient layout, then the 16-bit forms.
+        other = "planes" if layout == "media" else "media"
+        for key, f, lay in ((f"fp32-{other}", "fp32", other), ("fp16x", "fp16x", "planes"), ("fp16", "fp16", "planes")):
+            if f == form and (f != "fp32" or other == layout):
                 continue
             fk = max(1, min(K, args.form_steps))
-            fms, _, fbpc, _, _ = timed_run(prob, model, f, fk, W, group)
+            try:
+                fms, _, fbpc, _, _, flay = timed_run(prob, model, f, fk, W, group, layout=lay)
+            except Exception as exc:  # e.g. a model the media table cannot hold
+                forms[key] = {"error": f"{type(exc).__name__}: {exc}"[:200]}
+                continue
             fms = group.reduce(fms, "max")
-            forms[f] = {"value": round(ws * cells * fk / (fms / 1e3) / 1e6, 1), "ms_per_step": round(fms / fk, 4),
-                        "steps": fk, "bytes_per_cell": fbpc,
-                        "hbm_gbs": round(fbpc * cells / (fms / 1e3 / fk) / 1e9, 1)}
+            forms[key] = {"value": round(ws * cells * fk / (fms / 1e3) / 1e6, 1), "ms_per_step": round(fms / fk, 4),
+                          "steps": fk, "bytes_per_cell": fbpc, "coef_layout": flay,
+                          "hbm_gbs": round(fbpc * cells / (fms / 1e3 / fk) / 1e9, 1)}
         for f in forms:
-            forms[f]["speedup_vs_this_form"] = round((ms_max / K) / forms[f]["ms_per_step"], 3)
+            if "ms_per_step" in forms[f]:
+                forms[f]["speedup_vs_this_form"] = round((ms_max / K) / forms[f]["ms_per_step"], 3)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -351,7 +366,7 @@ def run_gb300(args, ws, rank, local, group):
         "config": {"workload": f"C1: {form.upper()} single shot, {prob.nx}^3 interior ({prob.sx}^3 grid), bord 4, "
                                f"absorb 32, dx 12.5 m, dt 0.6 ms, 8-layer seeded TTI, 15 Hz Ricker at {prob.src_xyz}",
                    "grid": [prob.sx, prob.sy, prob.sz], "updated_cells_per_step": cells,
-                   "form": form, "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "form": form, "coef_layout": layout, "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": f"inputs resident in HBM ({dev_gb:.1f} GB) are larger than L2 (129 MB); no flush",
                    "timed_steps_include": "fused source injection + one propagate launch per step"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -359,7 +374,7 @@ def run_gb300(args, ws, rank, local, group):
                      "algorithmic_bytes_per_cell": bpc,
                      "traffic": None if tpc is None else round(tpc * cells / 1e9, 3),
                      "traffic_unit": "GB per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
-                     "kernel": KERNEL[form]},
+                     "kernel": KERNEL[form] + (" (media-table layout)" if layout == "media" else "")},
         "e2e": None if e2e is None else {
                 "value": round(e2e, 1), "unit": UNIT, "h2d_bytes_per_step": int(stats[3] / KE),
                 "d2h_bytes_per_step": int(stats[4] / KE), "wall_s": round(e2e_wall, 3), "steps": KE,
@@ -623,6 +638,8 @@ def main():
     ap.add_argument("--abc-iters", type=int, default=3000, help="Adam steps of the learned layer's training")
     ap.add_argument("--abc-noise", type=float, default=0.0, help="input noise (std) in the learned layer's training")
     ap.add_argument("--no-forms", action="store_true", help="skip timing the other storage forms")
+    ap.add_argument("--coef-layout", default="planes", choices=["auto", "planes", "media"],
+                    help="coefficient layout of the FP32 form (the other one is timed under forms)")
     ap.add_argument("--form-steps", type=int, default=200, help="timed steps of each other storage form")
     ap.add_argument("--shots", type=int, default=48)
     ap.add_argument("--batch-form", default="fp32", choices=["fp32", "fp16", "fp16x"],

@@ -27,6 +27,8 @@ SIGNATURES = {
     "FLETCHER_GetStream": (C.c_void_p, []),
     "FLETCHER_SetForm": (C.c_int, [C.c_int]),
     "FLETCHER_SetNumerics": (C.c_int, [C.c_int]),
+    "FLETCHER_SetCoefLayout": (C.c_int, [C.c_int]),
+    "FLETCHER_CoefLayout": (C.c_int, []),
     "FLETCHER_InjectFault": (C.c_int, [C.c_int, C.c_int, C.c_int]),
     "FLETCHER_SetHostAccess": (C.c_int, [C.c_int]),
     "FLETCHER_HostAccess": (C.c_int, []),

@@ -20,6 +20,22 @@ enum DevCoef {
 constexpr int kArrivalCoef = 3;
 constexpr int kUpdateCoef = 7;
 
+// Media-table layout of the coefficients (FP32 form): the six angle terms
+// (DC_XX .. DC_YZ) depend on a cell's (phi, theta) only, so a model with at
+// most kMediaMax distinct (phi, theta) pairs stores them once per pair in a
+// table [6][kMediaMax] and one byte per cell (the pair's slot) in an id
+// volume [z][y][ipitch].  The id of cell x sits in byte x + kIdShift of its
+// row: a tile's first column kRadius + 32 t then starts at a multiple of 16
+// bytes, as a TMA load of 8-bit elements needs.  The four velocity terms
+// (DC_V2PX .. DC_V2PN) stay per cell in the coefficient block.
+constexpr int kMediaMax = 256;
+constexpr int kAngleCoef = 6;
+constexpr int kVelCoef = 4;
+constexpr int kIdShift = 12;
+constexpr int kMediaStages = 7;  // default pipeline depth of the media-table layout (fastest at 504^3)
+static_assert((kRadius + kIdShift) % 16 == 0 && kTileX % 16 == 0, "id tiles must start on 16-byte boundaries");
+static_assert(DC_V2PX == kAngleCoef && DC_V2PN == kNumCoef - 1, "velocity terms follow the angle terms");
+
 // One shot's geometry and buffers, in device memory (read by every launch).
 // The fields are stored as (p, q) pairs of float, [z][y][pitch] with x fastest.
 struct ShotDesc {
@@ -66,6 +82,7 @@ struct PropParams {
   unsigned int *err;                // error word (bit 0: bounded wait gave up)
   const int4 *seg;                  // single-shot launches with a segment list
   const int *cta_first;             // their [grid + 1] first segments
+  const float *media;               // media-table layout: angle terms [kAngleCoef][kMediaMax]
   unsigned long long wait_ns;       // limit of the step's waits (ns)
   int stall_step;                   // test hook: CTA 0 skips the loads of its stall_step-th step (-1: none)
 };
@@ -73,6 +90,7 @@ struct PropParams {
 // The four descriptors a single-shot launch passes as kernel parameters.
 struct SingleMaps {
   CUtensorMap cur_halo, prev_pt, arr, upd;
+  CUtensorMap ids, vel;  // media-table layout: id volume, box (TX, TY, 1); velocity terms, box (TX, TY, 4, 1)
 };
 
 struct PropLaunch {
@@ -80,6 +98,7 @@ struct PropLaunch {
   SingleMaps m;           // single-shot launches
   bool batch;             // true: p.shots / p.maps / p.items describe the work
   bool d1d1;              // Der1-Der1 numerics (single shot, 16 x 4 tiles)
+  bool media;             // media-table coefficient layout (single shot)
   int tile_rows;          // TY
   int stages;
   int grid;
@@ -87,6 +106,8 @@ struct PropLaunch {
 
 size_t propagate_fp32_smem_bytes(int tile_rows, int stages);
 bool propagate_fp32_supported(int tile_rows, int stages);
+// Shapes built for the media-table layout.
+bool propagate_fp32_media_supported(int tile_rows, int stages);
 int propagate_fp32_threads(int tile_rows);
 int propagate_fp32_ctas_per_sm(int tile_rows);
 cudaError_t propagate_fp32_prepare(int tile_rows, int stages);

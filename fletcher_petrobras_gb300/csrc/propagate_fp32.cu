@@ -24,6 +24,13 @@
 //  * plane k-4 is completed at step k and written with coalesced 64-bit
 //    stores into the previous-field buffer (in place).
 //
+// Media-table layout (template parameter MT): instead of the ten coefficient
+// planes a stage holds the one-byte medium ids of planes k and k-4 and the
+// four velocity terms of plane k-4; the six angle terms come from a table
+// of at most 256 media loaded into shared memory once per launch.  The
+// floats read are the same as in the plane layout, so results are
+// bit-identical; the stream drops from 64 to 41 bytes per cell.
+//
 // DerCross(p, a, b) equals D1_b(D1_a(p)) exactly in real arithmetic because
 // its weights are the products L_i L_j of the first-derivative weights
 // (original/derivatives.h:13-31); the FP32 rounding differs from the
@@ -34,20 +41,24 @@
 
 namespace flt {
 
-template <int TY, bool D1D1 = false>
+template <int TY, bool D1D1 = false, bool MT = false>
 struct Geo {
   static constexpr int TX = kTileX;
   static constexpr int HX = TX + 2 * kRadius;
   static constexpr int HY = TY + 2 * kRadius;
   static constexpr int NT = TX * TY;
   static constexpr int HALO_B = HX * HY * 8;
-  static constexpr int ARR_B = kArrivalCoef * NT * 4;
-  static constexpr int UPD_B = kUpdateCoef * NT * 4;
+  static constexpr int ARR_B = MT ? 0 : kArrivalCoef * NT * 4;
+  static constexpr int UPD_B = (MT ? kVelCoef : kUpdateCoef) * NT * 4;  // media table: velocity terms only
   static constexpr int PP_B = NT * 8;
+  static constexpr int ID_B = MT ? NT : 0;  // medium ids, one byte per cell
   static constexpr int OFF_ARR = HALO_B;
   static constexpr int OFF_UPD = OFF_ARR + ARR_B;
   static constexpr int OFF_PP = OFF_UPD + UPD_B;
-  static constexpr int STAGE_B = (OFF_PP + PP_B + 127) / 128 * 128;
+  static constexpr int OFF_IDC = OFF_PP + PP_B;  // ids of plane k
+  static constexpr int OFF_IDU = OFF_IDC + ID_B;  // ids of plane k-4
+  static constexpr int STAGE_B = (OFF_IDU + ID_B + 127) / 128 * 128;
+  static constexpr int TAB_B = MT ? kAngleCoef * kMediaMax * 4 : 0;
   // Exchange buffer, double-buffered: D1y of the tile rows with their 4-column
   // x halo, or (Der1-Der1 numerics) D1x of the tile columns with their 4-row
   // y halo.
@@ -60,13 +71,15 @@ struct Geo {
   static constexpr int AB_B = AB_SMEM ? 5 * NT * (D1D1 ? 24 : 16) : 0;
   static_assert(TY % 4 == 0, "tile rows must be a multiple of 4");
   static_assert(!D1D1 || (AB_SMEM && TY >= 8), "the Der1-Der1 numerics keep their in-plane terms in shared memory");
-  static_assert(HALO_B % 128 == 0 && ARR_B % 128 == 0 && UPD_B % 128 == 0, "stage regions 128-B aligned");
+  static_assert(HALO_B % 128 == 0 && ARR_B % 128 == 0 && UPD_B % 128 == 0 && ID_B % 128 == 0,
+                "stage regions 128-B aligned");
+  static_assert(!(MT && D1D1), "the Der1-Der1 numerics read the coefficient planes");
 };
 
-template <int TY, int S, bool D1D1 = false>
+template <int TY, int S, bool D1D1 = false, bool MT = false>
 constexpr size_t smem_bytes() {
-  using G = Geo<TY, D1D1>;
-  return size_t(S) * G::STAGE_B + G::DBUF_B + G::AB_B + 8 * S + 8 + 16 + 64 + 128;
+  using G = Geo<TY, D1D1, MT>;
+  return size_t(S) * G::STAGE_B + G::DBUF_B + G::AB_B + G::TAB_B + 8 * S + 8 + 16 + 64 + 128;
 }
 
 // A work item resolved against its shot: tile origin, z range, and (batched
@@ -128,9 +141,9 @@ __device__ __forceinline__ ItemRange item_range(const PropParams &P) {
   else return {(int)blockIdx.x, P.nitems, (int)gridDim.x};
 }
 
-// Descriptors used for one step of item `it`.
+// Descriptors used for one step of item `it` (ids, vel: media-table layout).
 struct StepMaps {
-  const CUtensorMap *cur, *prev, *arr, *upd;
+  const CUtensorMap *cur, *prev, *arr, *upd, *ids, *vel;
 };
 
 // The producer's position (next step to load), kept in shared memory so it
@@ -141,31 +154,45 @@ struct Cursor {
 };
 
 // Issues the TMA loads of one step (plane k of item `it`) into `stage`.
-template <int TY>
+// Media-table layout: the id tiles start at column x0 + kIdShift of the id
+// volume (x0 = kRadius + 32 t, so a multiple of 16 bytes).
+template <int TY, bool MT = false>
 __device__ __forceinline__ void issue_step(unsigned char *stage, uint64_t *bar, const Item &it, int k,
                                            const StepMaps &m) {
-  using G = Geo<TY>;
+  using G = Geo<TY, false, MT>;
   const bool center = (k >= it.z0) && (k < it.z1);
   const bool upd = (k - kRadius >= it.z0);
-  const uint32_t bytes = G::HALO_B + (center ? G::ARR_B : 0) + (upd ? G::UPD_B + G::PP_B : 0);
+  const uint32_t bytes =
+      G::HALO_B + (center ? G::ARR_B + G::ID_B : 0) + (upd ? G::UPD_B + G::PP_B + G::ID_B : 0);
   mbar_arrive_expect_tx(bar, bytes);
   tma_load_3d(stage, m.cur, bar, it.x0 - kRadius, it.y0 - kRadius, k);
-  if (center) tma_load_4d(stage + G::OFF_ARR, m.arr, bar, it.x0, it.y0, 0, k);
-  if (upd) {
-    tma_load_4d(stage + G::OFF_UPD, m.upd, bar, it.x0, it.y0, kArrivalCoef, k - kRadius);
-    tma_load_3d(stage + G::OFF_PP, m.prev, bar, it.x0, it.y0, k - kRadius);
+  if constexpr (MT) {
+    if (center) tma_load_3d(stage + G::OFF_IDC, m.ids, bar, it.x0 + kIdShift, it.y0, k);
+    if (upd) {
+      tma_load_4d(stage + G::OFF_UPD, m.vel, bar, it.x0, it.y0, DC_V2PX, k - kRadius);
+      tma_load_3d(stage + G::OFF_IDU, m.ids, bar, it.x0 + kIdShift, it.y0, k - kRadius);
+      tma_load_3d(stage + G::OFF_PP, m.prev, bar, it.x0, it.y0, k - kRadius);
+    }
+  } else {
+    if (center) tma_load_4d(stage + G::OFF_ARR, m.arr, bar, it.x0, it.y0, 0, k);
+    if (upd) {
+      tma_load_4d(stage + G::OFF_UPD, m.upd, bar, it.x0, it.y0, kArrivalCoef, k - kRadius);
+      tma_load_3d(stage + G::OFF_PP, m.prev, bar, it.x0, it.y0, k - kRadius);
+    }
   }
 }
 
 // D1D1: the Der1-Der1 numerics.  HOOK: the fault-injection variant (waits
 // limited to P.wait_ns, CTA 0 skipping the loads of step P.stall_step),
-// launched only when a test injects a stall.
-template <int TY, int S, bool ISO, int MODE, int MINB, bool D1D1 = false, bool HOOK = false>
+// launched only when a test injects a stall.  MT: the media-table layout of
+// the coefficients.
+template <int TY, int S, bool ISO, int MODE, int MINB, bool D1D1 = false, bool HOOK = false, bool MT = false>
 __global__ void __launch_bounds__(kTileX *TY, MINB)
     k_propagate_fp32(const __grid_constant__ SingleMaps SM, const __grid_constant__ PropParams P) {
   constexpr bool BATCH = MODE == kItemsBatch;
   static_assert(!D1D1 || (!ISO && !BATCH), "the Der1-Der1 numerics scale every derivative, single shot only");
-  using G = Geo<TY, D1D1>;
+  static_assert(!MT || (!BATCH && !HOOK && !D1D1), "the media-table layout runs single-shot plain steps");
+  using G = Geo<TY, D1D1, MT>;
   extern __shared__ unsigned char smem_dyn[];
   // Align in the shared window (pointer arithmetic on the shared array keeps
   // every access below a shared-memory access).
@@ -173,7 +200,8 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
   f2 *dbuf = reinterpret_cast<f2 *>(smem + S * G::STAGE_B);
   float4 *ABs = reinterpret_cast<float4 *>(smem + S * G::STAGE_B + G::DBUF_B);  // [5][NT] (AB_SMEM)
   f2 *Cs = reinterpret_cast<f2 *>(ABs + 5 * G::NT);  // [5][NT] (Der1-Der1 numerics: ch1dxy * pxy)
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem + S * G::STAGE_B + G::DBUF_B + G::AB_B);
+  float *s_med = reinterpret_cast<float *>(smem + S * G::STAGE_B + G::DBUF_B + G::AB_B);  // [6][256] (MT)
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + S * G::STAGE_B + G::DBUF_B + G::AB_B + G::TAB_B);
   uint64_t *xchg = full + S;  // D1y rows written (one arrival per warp)
   int *s_abort = reinterpret_cast<int *>(xchg + 1);
 
@@ -206,6 +234,8 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
       m.arr = &SM.arr;
       m.upd = &SM.upd;
     }
+    m.ids = &SM.ids;
+    m.vel = &SM.vel;
     return m;
   };
   Cursor *cur = reinterpret_cast<Cursor *>(s_abort + 4);
@@ -216,10 +246,10 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
     Cursor c = *cur;
     if constexpr (HOOK) {
       if (*s_issued != P.stall_step || blockIdx.x != 0)
-        issue_step<TY>(smem + c.stage * G::STAGE_B, &full[c.stage], c.it, c.k, maps_of(c.it));
+        issue_step<TY, MT>(smem + c.stage * G::STAGE_B, &full[c.stage], c.it, c.k, maps_of(c.it));
       ++*s_issued;
     } else {
-      issue_step<TY>(smem + c.stage * G::STAGE_B, &full[c.stage], c.it, c.k, maps_of(c.it));
+      issue_step<TY, MT>(smem + c.stage * G::STAGE_B, &full[c.stage], c.it, c.k, maps_of(c.it));
     }
     if (++c.stage == S) c.stage = 0;
     if (++c.k >= c.it.z1 + kRadius) {
@@ -251,6 +281,9 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
     *s_issued = 0;
     if constexpr (MODE != kItemsTiles) *s_end = R.end;
   }
+  if constexpr (MT) {
+    for (int i = tid; i < kAngleCoef * kMediaMax; i += kTileX * TY) s_med[i] = P.media[i];
+  }
   if (producer) {
     Cursor c;
     c.it = decode_item<TY, MODE>(R.first, P);
@@ -265,8 +298,13 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
       const StepMaps m = maps_of(cur->it);
       tma_prefetch_desc(m.cur);
       tma_prefetch_desc(m.prev);
-      tma_prefetch_desc(m.arr);
-      tma_prefetch_desc(m.upd);
+      if constexpr (MT) {
+        tma_prefetch_desc(m.ids);
+        tma_prefetch_desc(m.vel);
+      } else {
+        tma_prefetch_desc(m.arr);
+        tma_prefetch_desc(m.upd);
+      }
       if (BATCH && cur->item + 1 < item_end()) {
         const StepMaps m2 = maps_of(decode_item<TY, MODE>(cur->item + 1, P));
         tma_prefetch_desc(m2.cur);
@@ -437,9 +475,25 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
 #undef RX
 #undef RY
           const float *cu = reinterpret_cast<const float *>(st + G::OFF_UPD);
-          const float czz = cu[ci], cxz = cu[G::NT + ci], cyz = cu[2 * G::NT + ci];
-          const float v2px = cu[3 * G::NT + ci], v2pz = cu[4 * G::NT + ci];
-          const float v2sz = cu[5 * G::NT + ci], v2pn = cu[6 * G::NT + ci];
+          float czz, cxz, cyz, v2px, v2pz, v2sz, v2pn;
+          if constexpr (MT) {
+            const int md = st[G::OFF_IDU + ci];
+            czz = s_med[(DC_ZZ * kMediaMax) + md];
+            cxz = s_med[(DC_XZ * kMediaMax) + md];
+            cyz = s_med[(DC_YZ * kMediaMax) + md];
+            v2px = cu[ci];
+            v2pz = cu[G::NT + ci];
+            v2sz = cu[2 * G::NT + ci];
+            v2pn = cu[3 * G::NT + ci];
+          } else {
+            czz = cu[ci];
+            cxz = cu[G::NT + ci];
+            cyz = cu[2 * G::NT + ci];
+            v2px = cu[3 * G::NT + ci];
+            v2pz = cu[4 * G::NT + ci];
+            v2sz = cu[5 * G::NT + ci];
+            v2pn = cu[6 * G::NT + ci];
+          }
           f2 Ak, Bk;
           if constexpr (G::AB_SMEM) {
             const float4 ab = ABs[(abw == 4 ? 0 : abw + 1) * G::NT + ci];
@@ -512,8 +566,18 @@ __global__ void __launch_bounds__(kTileX *TY, MINB)
         } else if (center) {
           const f2 *dr = db + ly * G::HX + lx + kRadius;
           const f2 dxy = scale<ISO>(d1(dr[1], dr[-1], dr[2], dr[-2], dr[3], dr[-3], dr[4], dr[-4]), sxy);
-          const float *ca = reinterpret_cast<const float *>(st + G::OFF_ARR);
-          const float cxx = ca[ci], cyy = ca[G::NT + ci], cxy = ca[2 * G::NT + ci];
+          float cxx, cyy, cxy;
+          if constexpr (MT) {
+            const int md = st[G::OFF_IDC + ci];
+            cxx = s_med[(DC_XX * kMediaMax) + md];
+            cyy = s_med[(DC_YY * kMediaMax) + md];
+            cxy = s_med[(DC_XY * kMediaMax) + md];
+          } else {
+            const float *ca = reinterpret_cast<const float *>(st + G::OFF_ARR);
+            cxx = ca[ci];
+            cyy = ca[G::NT + ci];
+            cxy = ca[2 * G::NT + ci];
+          }
           const f2 av = fma2(splat(cxy), dxy, fma2(splat(cyy), d2y, mul2(splat(cxx), d2x)));
           const f2 bv = add2(d2x, d2y);
           if constexpr (G::AB_SMEM) {
@@ -639,16 +703,59 @@ static cudaError_t launch_hook(const PropLaunch &L, cudaStream_t s) {
     }
     ready = true;
   }
-  if (L.batch || L.d1d1 || L.tile_rows != TY || L.stages != S) return cudaErrorInvalidValue;
+  // Any pipeline depth of the step's own shape: the plan depends on the rows
+  // only.  (The coefficient planes are present in either layout.)
+  if (L.batch || L.d1d1 || L.tile_rows != TY) return cudaErrorInvalidValue;
   const bool iso = L.p.iso != 0;
   auto kern = L.p.seg ? (iso ? segs_i : segs_a) : (iso ? tiles_i : tiles_a);
   kern<<<L.grid, kTileX * TY, smem, s>>>(L.m, L.p);
   return cudaGetLastError();
 }
 
+// The media-table layout: single shot, 16-row tiles.
+#define FLT_MEDIA_SHAPES(X) X(16, 5) X(16, 6) X(16, 7)
+
+template <int TY, int S>
+static cudaError_t launch_media_t(const PropLaunch &L, cudaStream_t s) {
+  constexpr size_t smem = smem_bytes<TY, S, false, true>();
+  static_assert(smem <= 227 * 1024, "media-table shape exceeds the shared memory of a CTA");
+  auto tiles_i = k_propagate_fp32<TY, S, true, kItemsTiles, 1, false, false, true>;
+  auto tiles_a = k_propagate_fp32<TY, S, false, kItemsTiles, 1, false, false, true>;
+  auto segs_i = k_propagate_fp32<TY, S, true, kItemsSegments, 1, false, false, true>;
+  auto segs_a = k_propagate_fp32<TY, S, false, kItemsSegments, 1, false, false, true>;
+  static bool ready = false;
+  if (!ready) {
+    for (auto kern : {tiles_i, tiles_a, segs_i, segs_a}) {
+      const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    ready = true;
+  }
+  const bool iso = L.p.iso != 0;
+  auto kern = L.p.seg ? (iso ? segs_i : segs_a) : (iso ? tiles_i : tiles_a);
+  kern<<<L.grid, kTileX * TY, smem, s>>>(L.m, L.p);
+  return cudaGetLastError();
+}
+
+bool propagate_fp32_media_supported(int ty, int st) {
+#define X(a, b) \
+  if (ty == a && st == b) return true;
+  FLT_MEDIA_SHAPES(X)
+#undef X
+  return false;
+}
+
 cudaError_t propagate_fp32_launch(const PropLaunch &L, cudaStream_t s) {
   if (L.p.stall_step >= 0) return launch_hook(L, s);
   if (L.d1d1) return launch_d1d1(L, s);
+  if (L.media) {
+    if (L.batch || !L.p.media) return cudaErrorInvalidValue;
+#define X(a, b) \
+  if (L.tile_rows == a && L.stages == b) return launch_media_t<a, b>(L, s);
+    FLT_MEDIA_SHAPES(X)
+#undef X
+    return cudaErrorInvalidValue;
+  }
 #define X(a, b, c) \
   if (L.tile_rows == a && L.stages == b) return launch_t<a, b, c>(L, s);
   FLT_SHAPES(X)

@@ -127,6 +127,37 @@ int FLETCHER_SetForm(int form);
 #define FLETCHER_NUMERICS_D1D1 1
 int FLETCHER_SetNumerics(int mode);
 
+/* Device layout of the ten coefficient fields of the FP32 form (original/
+ * precomp.h:14-58), chosen before DRIVER_Initialize.  No counterpart in the
+ * reference, which streams all ten per cell.
+ * FLETCHER_COEF_PLANES (default): ten FP32 planes per z-plane; a step
+ *   streams 64 bytes per cell (24 of fields, 40 of coefficients).
+ * FLETCHER_COEF_MEDIA: the six angle coefficients depend on a cell's
+ *   (phi, theta) only; a model with at most 256 distinct (phi, theta) bit
+ *   pairs keeps them in a table, one byte per cell names the pair, and a
+ *   step streams 41 bytes per cell (the four velocity coefficients stay per
+ *   cell).  The floats used are the same, so results are bit-identical to
+ *   FLETCHER_COEF_PLANES.  16-row tiles of 5, 6 or 7 stages (default 7).
+ *   On GB300 at 504^3 it streams 36% fewer bytes but runs 3-5% slower than
+ *   the planes (the step's limit is its per-plane chain of shared-memory
+ *   reads, which the table lengthens, not DRAM); it leaves more HBM
+ *   bandwidth to other work on the GPU.
+ *   DRIVER_Initialize fails with FLETCHER_ERR_ARGS when the model has more
+ *   pairs, or with a 16-bit form or the Der1-Der1 numerics.
+ * FLETCHER_COEF_AUTO: FLETCHER_COEF_MEDIA where the form, the numerics,
+ *   the requested tile shape and the model allow it, else
+ *   FLETCHER_COEF_PLANES.
+ * FLETCHER_CoefLayout: the layout of the initialised state (PLANES or
+ *   MEDIA), or a negative status before DRIVER_Initialize.
+ * Tuning files (FLETCHER_Autotune) keep the media-table layout's shapes
+ * under the form key FLETCHER_TUNE_FP32_MEDIA ("fp32-media"). */
+#define FLETCHER_COEF_AUTO 0
+#define FLETCHER_COEF_PLANES 1
+#define FLETCHER_COEF_MEDIA 2
+#define FLETCHER_TUNE_FP32_MEDIA 3
+int FLETCHER_SetCoefLayout(int layout);
+int FLETCHER_CoefLayout(void);
+
 /* Fault injection for tests of the failure paths (no counterpart in the
  * reference, whose back-ends exit on any error).  Nothing here faults or
  * hangs the GPU.
@@ -210,9 +241,10 @@ long FLETCHER_KernelLaunches(void);
 /* Device bytes held by the current state. */
 size_t FLETCHER_DeviceBytes(void);
 
-/* Algorithmic HBM bytes one updated cell costs in the current form (reads
- * of the current and previous fields and the coefficients, writes of the
- * next field). */
+/* Algorithmic HBM bytes one updated cell costs in the current form and
+ * coefficient layout (reads of the current and previous fields and the
+ * coefficients -- or, in the media-table layout, the four velocity
+ * coefficients and the id byte -- and writes of the next field). */
 double FLETCHER_BytesPerCell(void);
 
 /* ---- Output path (original/utils.c:7-227, original/model.c:98-107).

@@ -128,12 +128,13 @@ def run_f32(prob, model: np.ndarray, steps: int | None = None, coef: np.ndarray 
     return (pp, qp, pc, qc) if odd else (pc, qc, pp, qp)
 
 
-def run_d1d1_f32(prob, model: np.ndarray, steps: int | None = None):
-    """FP32 oracle run of the Der1-Der1 formulation (der1der1/ tree);
+def run_d1d1_f32(prob, model: np.ndarray, steps: int | None = None, coef: np.ndarray | None = None):
+    """FP32 oracle run of the Der1-Der1 formulation (der1der1/ tree), with the
+    given coefficients (default: the reference's precompute of `model`);
     returns (p, q, pp, qp) final current/previous fields."""
     lib = load()
     st = prob.steps if steps is None else steps
-    coef = precompute(model)
+    coef = precompute(model) if coef is None else np.ascontiguousarray(coef, np.float32).reshape(10, -1)
     n = prob.n
     pp, pc, qp, qc = (np.zeros(n, np.float32) for _ in range(4))
     odd = lib.orc_run_d1d1_f32(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, st,

@@ -78,3 +78,42 @@ def test_d1d1_numerics_rejects_16bit_forms():
     with pytest.raises(FletcherError, match="FP32 form"):
         prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, prob.model())
     Propagator(form="fp32", numerics="fast")
+
+
+@pytest.mark.parametrize("case", ["odd_sizes", "bord6", "thin_z", "src_tile_edge", "src_in_border"])
+def test_d1d1_numerics_edge_cases_bit_identical_to_oracle(case, orc):
+    """The geometry and source edge cases of the default numerics' parity tests
+    (grid not a multiple of the tile, a border wider than the stencil, a few
+    planes only, a source on a tile corner and chunk edge, a source in the
+    never-updated border), held to bit equality against the oracle's
+    restatement of the der1der1/ tree -- given the same coefficients: the
+    GPU's FP64 trigonometry can round a coefficient one unit differently from
+    the host's, which is not what this test is about."""
+    base = Problem("edge", 21, 13, 9, absorb=3, dt=0.0006, steps=20, fcut=45.0, kind="layered", layers=3, seed=4)
+    zc = 0
+    if case == "odd_sizes":
+        prob = base
+    elif case == "bord6":
+        prob = base.with_(bord=6)
+    elif case == "thin_z":
+        prob, zc = base.with_(nz=1, nx=40, ny=37), 3
+    elif case == "src_tile_edge":
+        prob = Problem("edge2", 60, 40, 40, absorb=4, dt=0.0006, steps=20, fcut=45.0, seed=4)
+        prob, zc = prob.with_(source=(4 + 32, 4 + 15, 4 + 13)), 3  # tile corner (16-row tiles), chunk edge
+    else:
+        prob = base.with_(source=(2, base.sy // 2, base.sz // 2))
+    m = prob.model()
+    prop = Propagator(zchunks=zc, numerics="d1d1")
+    prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, m)
+    src = prob.sources()
+    for it in range(1, prob.steps + 1):
+        prop.insert_source(it - 1, prob.i_source, src[it - 1])
+        prop.propagate(it)
+    got = [prop.field(k) for k in range(4)]
+    coef = prop.coefficients()
+    prop.finalize()
+    Propagator(numerics="fast")
+    want = orc.run_d1d1_f32(prob, m, coef=coef)
+    assert np.abs(want[0]).max() > 0
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w), rel_l2(g, w)
