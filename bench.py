@@ -295,7 +295,11 @@ def run_gb300(args, ws, rank, local, group):
     e2e = e2e_wall = parity = e2e_clk = None
     KE = args.e2e_steps or prob.steps  # the workload's own step count (1000 at C1)
     if not args.no_e2e:
-        f = np.zeros((4, prob.n), np.float32)
+        # The initial fields are written (zeroed) by the caller before the
+        # call, as the reference's main() does (original/main.c:257-258); pages
+        # never written would make locking them for the copies allocate them.
+        f = np.empty((4, prob.n), np.float32)
+        f.fill(0.0)
         from fletcher_petrobras_gb300.driver import FORMS
 
         from fletcher_petrobras_gb300.driver import COEF_LAYOUTS
@@ -316,6 +320,8 @@ def run_gb300(args, ws, rank, local, group):
         lib.FLETCHER_SetCoefLayout(COEF_LAYOUTS["planes"])
         phases = (C.c_double * 4)()
         lib.FLETCHER_ModelPhases(phases)
+        init_phases = (C.c_double * 5)()
+        lib.FLETCHER_InitPhases(init_phases)
         e2e_wall = group.reduce(stats[2], "max")
         e2e = ws * cells * KE / e2e_wall / 1e6
         parity = reference_parity(prob, KE, form, f[1], f[3])  # FLETCHER_Model leaves the final p, q in pc, qc
@@ -380,6 +386,8 @@ def run_gb300(args, ws, rank, local, group):
                 "d2h_bytes_per_step": int(stats[4] / KE), "wall_s": round(e2e_wall, 3), "steps": KE,
                 "phases_s": {"setup": round(phases[0], 3), "steps": round(phases[1], 3),
                              "snapshot_drain": round(phases[2], 3), "readback_finalize": round(phases[3], 3)},
+                "setup_phases_s": dict(zip(("alloc", "lock_and_issue_copies", "device_work", "plan_and_maps",
+                                            "unlock"), (round(v, 4) for v in init_phases))),
                 "clocks": e2e_clk,
                 "what": f"FLETCHER_Model via the C ABI, the workload's {KE} steps: DRIVER_Initialize (H2D of 6 "
                         "model + 4 field arrays, FP64 coefficient precompute) + per step (InsertSource, Propagate) "

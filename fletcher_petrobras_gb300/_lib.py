@@ -29,6 +29,7 @@ SIGNATURES = {
     "FLETCHER_SetNumerics": (C.c_int, [C.c_int]),
     "FLETCHER_SetCoefLayout": (C.c_int, [C.c_int]),
     "FLETCHER_CoefLayout": (C.c_int, []),
+    "FLETCHER_InitPhases": (C.c_int, [DP]),
     "FLETCHER_InjectFault": (C.c_int, [C.c_int, C.c_int, C.c_int]),
     "FLETCHER_SetHostAccess": (C.c_int, [C.c_int]),
     "FLETCHER_HostAccess": (C.c_int, []),

@@ -25,6 +25,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <vector>
 
 #include "../../include/fletcher_gb300.h"
@@ -107,6 +108,13 @@ int g_errmode = FLETCHER_ERRMODE_EXIT;
 // the copies measured faster (e2e 66.3 vs 49.2 GMSamples/s at 504^3).
 int g_host_access = 0;
 int g_numerics = FLETCHER_NUMERICS_FAST;
+// Wall-clock marks of the last DRIVER_Initialize (FLETCHER_InitPhases):
+// start, allocations done, host arrays locked and copies issued, device work
+// done, state ready, arrays unlocked.
+double g_init_mark[6];
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
 // Coefficient layout of the FP32 form (FLETCHER_SetCoefLayout).  The plane
 // layout is the default: at 504^3 the media table, with 36% fewer bytes per
 // step, ran 3-5% slower (2.30-2.48 against 2.22 ms per step; the step is
@@ -801,6 +809,7 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   CK(cudaHostGetDevicePointer((void **)&g.err_dev, g.err_host, 0));
   g.dev_bytes += g.npitch * kNumCoef * sizeof(float) + g.n * sizeof(float);
   CK(cudaMemsetAsync(g.coef, 0, g.npitch * kNumCoef * sizeof(float), s));
+  g_init_mark[1] = now_s();
 
   // Raw model arrays -> coefficients.  On systems whose GPU reads pageable
   // host memory (Grace over NVLink-C2C) the kernels read the caller's arrays
@@ -824,6 +833,7 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
     }
     for (const float *f : {pp, pc, qp, qc}) pins.add(f, g.n * sizeof(float));
   }
+  g_init_mark[2] = now_s();
   const unsigned long long all_finite = ~0ull;
   CK(cudaMemcpyToSymbolAsync(g_bad_model, &all_finite, sizeof(all_finite), 0, cudaMemcpyHostToDevice, s));
   k_precompute<<<grid_for(g.n), 256, 0, s>>>(r6, g.coef, sx, sy, sz, g.pitch);
@@ -872,6 +882,7 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
     }
   }
   CK(cudaStreamSynchronize(s));
+  g_init_mark[3] = now_s();
   if (raw) CK(cudaFree(raw));
   unsigned long long bad = 0;
   CK(cudaMemcpyFromSymbol(&bad, g_bad_model, sizeof(bad)));
@@ -911,6 +922,7 @@ int initialize(int sx, int sy, int sz, int bord, float dx, float dy, float dz, f
   g.pending = Source();
   g.owed = Source();
   g.init = true;
+  g_init_mark[4] = now_s();
   return FLETCHER_OK;
 }
 
@@ -1127,9 +1139,19 @@ cudaStream_t resident_stream() { return g_stream; }
 extern "C" void DRIVER_Initialize(const int sx, const int sy, const int sz, const int bord, float dx, float dy,
                                   float dz, float dt, float *vpz, float *vsv, float *epsilon, float *delta,
                                   float *phi, float *theta, float *pp, float *pc, float *qp, float *qc) {
+  for (double &m : g_init_mark) m = 0.0;
+  g_init_mark[0] = now_s();
   if (initialize(sx, sy, sz, bord, dx, dy, dz, dt, vpz, vsv, epsilon, delta, phi, theta, pp, pc, qp, qc) !=
       FLETCHER_OK)
     free_state();
+  g_init_mark[5] = now_s();
+}
+
+extern "C" int FLETCHER_InitPhases(double *out) {
+  if (!out) return fail(FLETCHER_ERR_ARGS, "FLETCHER_InitPhases: NULL output");
+  for (int k = 0; k < 5; ++k)
+    out[k] = g_init_mark[k + 1] > 0.0 && g_init_mark[k] > 0.0 ? g_init_mark[k + 1] - g_init_mark[k] : 0.0;
+  return FLETCHER_OK;
 }
 
 extern "C" void DRIVER_Finalize(void) {

@@ -238,6 +238,13 @@ int FLETCHER_GetCoefficients(float *host);
 /* Number of propagate-kernel launches issued since DRIVER_Initialize. */
 long FLETCHER_KernelLaunches(void);
 
+/* Wall-clock phases (s) of the last successful DRIVER_Initialize, in out[5]:
+ * device allocations; locking the caller's host arrays and issuing their
+ * copies; the device work (copies, coefficient precompute, field packing)
+ * until it completes; tile planning and tensor maps; unlocking the host
+ * arrays.  Zero where the call stopped early. */
+int FLETCHER_InitPhases(double *out);
+
 /* Device bytes held by the current state. */
 size_t FLETCHER_DeviceBytes(void);
 
