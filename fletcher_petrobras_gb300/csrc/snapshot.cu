@@ -41,12 +41,17 @@ __global__ void k_gather_box(const float *__restrict__ v, float *__restrict__ ou
 
 namespace {
 
+// Two device buffers of one unpacked field each, used in turn by the
+// full-field snapshots: a snapshot waits only for the copy out of the buffer
+// it reuses, two snapshots back, so a copy that runs longer than the steps
+// between two snapshots does not hold up the steps.  Slices use buffer 0.
 struct Snap {
   cudaStream_t side = nullptr;
-  float *dev = nullptr;      // one unpacked field
+  float *dev[2] = {nullptr, nullptr};
   float *staging = nullptr;  // page-locked, for unregistered destinations
   size_t n = 0;
-  cudaEvent_t dev_free = nullptr, ready = nullptr, done = nullptr;
+  cudaEvent_t dev_free[2] = {nullptr, nullptr}, ready = nullptr, done = nullptr;
+  int next = 0;              // buffer of the next full-field snapshot
   bool inflight = false;
 };
 Snap S;
@@ -66,20 +71,23 @@ int err(int code, const char *msg) { return flt_record_error(code, msg); }
 int ensure(size_t n) {
   if (!S.side) {
     CKS(cudaStreamCreateWithFlags(&S.side, cudaStreamNonBlocking));
-    CKS(cudaEventCreateWithFlags(&S.dev_free, cudaEventDisableTiming));
+    for (int k = 0; k < 2; ++k) CKS(cudaEventCreateWithFlags(&S.dev_free[k], cudaEventDisableTiming));
     CKS(cudaEventCreateWithFlags(&S.ready, cudaEventDisableTiming));
     CKS(cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming));
   }
   if (S.n != n) {
     if (S.inflight) CKS(cudaEventSynchronize(S.done));
-    if (S.dev) cudaFree(S.dev);
+    for (int k = 0; k < 2; ++k) {
+      if (S.dev[k]) cudaFree(S.dev[k]);
+      S.dev[k] = nullptr;
+    }
     if (S.staging) cudaFreeHost(S.staging);
-    S.dev = nullptr;
     S.staging = nullptr;
     S.n = 0;
-    CKS(cudaMalloc(&S.dev, n * sizeof(float)));
+    for (int k = 0; k < 2; ++k) CKS(cudaMalloc(&S.dev[k], n * sizeof(float)));
     S.n = n;
-    CKS(cudaEventRecord(S.dev_free, resident_stream()));
+    S.next = 0;
+    for (int k = 0; k < 2; ++k) CKS(cudaEventRecord(S.dev_free[k], resident_stream()));
   }
   return FLETCHER_OK;
 }
@@ -112,9 +120,11 @@ void CUDART_CB copy_out(void *arg) {
 
 void snapshot_release() {
   if (S.side) cudaStreamSynchronize(S.side);
-  if (S.dev) cudaFree(S.dev);
+  for (int k = 0; k < 2; ++k) {
+    if (S.dev[k]) cudaFree(S.dev[k]);
+    S.dev[k] = nullptr;
+  }
   if (S.staging) cudaFreeHost(S.staging);
-  S.dev = nullptr;
   S.staging = nullptr;
   S.n = 0;
   S.inflight = false;
@@ -132,23 +142,27 @@ extern "C" int FLETCHER_SnapshotBegin(int which, float *host) {
   if (!host || which < 0 || which > 3) return err(FLETCHER_ERR_ARGS, "FLETCHER_SnapshotBegin: bad arguments");
   if (ensure(n)) return FLETCHER_GetLastError();
   cudaStream_t s = resident_stream();
-  // The previous copy out of the device buffer must be done before it is
-  // overwritten (a device-side wait; the host does not block).
-  CKS(cudaStreamWaitEvent(s, S.dev_free, 0));
+  const int k = S.next;
+  S.next ^= 1;
+  // The copy out of this buffer two snapshots back must be done before it
+  // is overwritten (a device-side wait; the host does not block).
+  CKS(cudaStreamWaitEvent(s, S.dev_free[k], 0));
   long fix_idx = -1;
   float fix_val = 0.f;
-  if (resident_field_to_device(which, S.dev, &fix_idx, &fix_val)) return FLETCHER_GetLastError();
+  if (resident_field_to_device(which, S.dev[k], &fix_idx, &fix_val)) return FLETCHER_GetLastError();
   CKS(cudaEventRecord(S.ready, s));
   CKS(cudaStreamWaitEvent(S.side, S.ready, 0));
   CopyOut *c = new CopyOut{host, nullptr, n, fix_idx, fix_val};
   if (page_locked(host)) {
-    CKS(cudaMemcpyAsync(host, S.dev, n * sizeof(float), cudaMemcpyDeviceToHost, S.side));
+    CKS(cudaMemcpyAsync(host, S.dev[k], n * sizeof(float), cudaMemcpyDeviceToHost, S.side));
   } else {
+    // One staging buffer: the side stream runs its copies and host-side
+    // copy-outs in order, so a staging copy never overtakes the last one.
     if (!S.staging) CKS(cudaHostAlloc(&S.staging, n * sizeof(float), cudaHostAllocDefault));
-    CKS(cudaMemcpyAsync(S.staging, S.dev, n * sizeof(float), cudaMemcpyDeviceToHost, S.side));
+    CKS(cudaMemcpyAsync(S.staging, S.dev[k], n * sizeof(float), cudaMemcpyDeviceToHost, S.side));
     c->src = S.staging;
   }
-  CKS(cudaEventRecord(S.dev_free, S.side));
+  CKS(cudaEventRecord(S.dev_free[k], S.side));
   if (c->src || c->fix_idx >= 0) {
     CKS(cudaLaunchHostFunc(S.side, copy_out, c));
   } else {
@@ -297,17 +311,17 @@ extern "C" int FLETCHER_SliceAppend(FletcherSlice *s, int which) {
     CKS(cudaEventRecord(s->dev_free, resident_stream()));
   }
   cudaStream_t st = resident_stream();
-  CKS(cudaStreamWaitEvent(st, S.dev_free, 0));
+  CKS(cudaStreamWaitEvent(st, S.dev_free[0], 0));
   CKS(cudaStreamWaitEvent(st, s->dev_free, 0));
   long fi;
   float fv;
-  if (resident_field_to_device(which, S.dev, &fi, &fv)) return FLETCHER_GetLastError();
+  if (resident_field_to_device(which, S.dev[0], &fi, &fv)) return FLETCHER_GetLastError();
   const int nx = s->x1 - s->x0 + 1, ny = s->y1 - s->y0 + 1, nz = s->z1 - s->z0 + 1;
   long blocks = ((long)s->count + 255) / 256;
-  k_gather_box<<<(int)(blocks < 4096 ? blocks : 4096), 256, 0, st>>>(S.dev, s->dev, sx, sy, s->x0, nx, s->y0, ny,
-                                                                     s->z0, nz);
+  k_gather_box<<<(int)(blocks < 4096 ? blocks : 4096), 256, 0, st>>>(S.dev[0], s->dev, sx, sy, s->x0, nx, s->y0,
+                                                                     ny, s->z0, nz);
   CKS(cudaGetLastError());
-  CKS(cudaEventRecord(S.dev_free, st));
+  CKS(cudaEventRecord(S.dev_free[0], st));
   CKS(cudaEventRecord(S.ready, st));
   CKS(cudaStreamWaitEvent(S.side, S.ready, 0));
   CKS(cudaMemcpyAsync(s->staging, s->dev, s->count * sizeof(float), cudaMemcpyDeviceToHost, S.side));

@@ -106,3 +106,47 @@ def test_model_loop_snapshots_land_in_the_callers_arrays():
     prop2.finalize()
     assert np.array_equal(f[1], want_p) and np.array_equal(f[3], want_q)
     assert stats[4] > 2 * 4 * p.n  # snapshots were taken
+
+
+def test_consecutive_snapshots_each_hold_their_step(tmp_path, monkeypatch):
+    """Snapshots one step apart use the two device buffers in turn (and a
+    slice append in between uses the first): each copy still holds the field
+    of its own step, while the steps after it run."""
+    prop = start("fp32")
+    lib = prop.lib
+    p = PROB
+    monkeypatch.chdir(tmp_path)
+    src = p.sources()
+    n = p.n
+    at = [5, 6, 7, 9]
+    outs = [np.full(n, np.nan, np.float32) for _ in at]
+    box = (4, p.sx - 5, 4, p.sy - 5, p.sz // 2, p.sz // 2)  # a z-slice
+    sl = lib.FLETCHER_OpenSliceFile(*box, p.dx, p.dy, p.dz, p.dt, b"mid")
+    done = 0
+    for i, step in enumerate(at):
+        prop.run(step - done, p.i_source, src[done:step])
+        done = step
+        assert lib.FLETCHER_SnapshotBegin(0, fptr(outs[i])) == 0
+        if i == 1:
+            assert lib.FLETCHER_SliceAppend(sl, 0) == 0
+    prop.run(10, p.i_source, src[done:done + 10])
+    assert lib.FLETCHER_SnapshotWait() == 0
+    assert lib.FLETCHER_CloseSliceFile(sl) == 0
+    prop.finalize()
+    prop = start("fp32")
+    want = []
+    done = 0
+    for step in at:
+        prop.run(step - done, p.i_source, src[done:step])
+        done = step
+        want.append(prop.field(0))
+    prop.finalize()
+    for o, w in zip(outs, want):
+        assert np.array_equal(o, w)
+    # The slice holds step 6: the host writer on that step's field gives the same file.
+    h = lib.FLETCHER_OpenSliceFile(*box, p.dx, p.dy, p.dz, p.dt, b"ref")
+    assert lib.FLETCHER_DumpSliceFile(p.sx, p.sy, p.sz, fptr(want[1]), h) == 0
+    assert lib.FLETCHER_CloseSliceFile(h) == 0
+    x = open(os.path.join(tmp_path, "mid.rsf@"), "rb").read()
+    y = open(os.path.join(tmp_path, "ref.rsf@"), "rb").read()
+    assert len(x) == 4 * (box[1] - box[0] + 1) * (box[3] - box[2] + 1) and x == y
