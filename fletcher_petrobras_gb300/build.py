@@ -28,7 +28,7 @@ C_FLAGS = ["-O3", "-fPIC", "-ffp-contract=off", "-std=gnu11", "-Wall", "-I" + IN
 
 CU_SOURCES = ["driver.cu", "propagate_fp32.cu", "propagate_half.cu", "abc_learned.cu", "snapshot.cu", "noalloc.cu"]
 C_SOURCES = ["host/fletcher_host.c"]
-HEADERS = ["device_util.cuh", "fletcher_internal.h", "stencil_common.cuh"]
+HEADERS = ["device_util.cuh", "fletcher_internal.h", "stencil_common.cuh", "propagate_fp32_pipe.cuh"]
 
 
 def _newer(target: str, deps: list[str]) -> bool:
