@@ -46,6 +46,8 @@ SIGNATURES = {
     "FLETCHER_BatchAddShot": (C.c_int, [C.c_int] * 3 + [FP, C.c_long, C.c_int]),
     "FLETCHER_BatchSetTileConfig": (C.c_int, [C.c_int, C.c_int]),
     "FLETCHER_BatchRun": (C.c_int, [FP, C.c_int, C.c_int, FP]),
+    "FLETCHER_BatchSetChains": (C.c_int, [C.c_int]),
+    "FLETCHER_BatchLastChains": (C.c_int, []),
     "FLETCHER_BatchReset": (C.c_int, []),
     "FLETCHER_BatchGetField": (C.c_int, [C.c_int, C.c_int, FP]),
     "FLETCHER_BatchInfo": (C.c_int, [C.POINTER(C.c_long), DP, C.POINTER(C.c_long), C.POINTER(C.c_size_t)]),

@@ -38,8 +38,10 @@ def multishot_spec(nshots: int = 48, seed: int = 0, nmin: int = 96, nmax: int = 
 class Batch:
     """A batch of shots resident on the GPU (one per process)."""
 
-    def __init__(self, bord=4, dx=12.5, dy=12.5, dz=12.5, dt=0.0006, form: str = "fp32"):
-        """form: storage form of every shot's fields ("fp32", "fp16", "fp16x")."""
+    def __init__(self, bord=4, dx=12.5, dy=12.5, dz=12.5, dt=0.0006, form: str = "fp32", chains: int | None = None):
+        """form: storage form of every shot's fields ("fp32", "fp16", "fp16x").
+        chains: schedule of an FP32 batch (FLETCHER_BatchSetChains; None keeps
+        the library's default)."""
         self.lib = _lib.load()
         self.lib.FLETCHER_ClearError()
         if form not in FORMS:
@@ -49,6 +51,8 @@ class Batch:
             _check(self.lib, "SetForm")
         if self.lib.FLETCHER_BatchCreate(bord, dx, dy, dz, dt):
             _check(self.lib, "FLETCHER_BatchCreate")
+        if chains is not None and self.lib.FLETCHER_BatchSetChains(int(chains)):
+            _check(self.lib, "FLETCHER_BatchSetChains")
         self.dt = dt
         self.probs = []
 
@@ -90,7 +94,8 @@ class Batch:
     def info(self) -> dict:
         ns, cs, la, db = C.c_long(0), C.c_double(0), C.c_long(0), C.c_size_t(0)
         self.lib.FLETCHER_BatchInfo(C.byref(ns), C.byref(cs), C.byref(la), C.byref(db))
-        return {"shots": ns.value, "cell_steps": cs.value, "launches": la.value, "device_bytes": db.value}
+        return {"shots": ns.value, "cell_steps": cs.value, "launches": la.value, "device_bytes": db.value,
+                "chains": self.lib.FLETCHER_BatchLastChains()}
 
     def close(self):
         self.lib.FLETCHER_BatchDestroy()

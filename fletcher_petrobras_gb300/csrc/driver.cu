@@ -1521,6 +1521,23 @@ struct Batch {
   int num_sms = 0;
   unsigned *err_host = nullptr, *err_dev = nullptr;
   std::vector<float> src;      // source values of the last run
+  // Chain schedule (FP32, chains > 0, FLETCHER_BatchSetChains): every step
+  // of a shot is a single-shot launch; the shots are dealt over `chains`
+  // concurrent streams, each running its shots one after another.  Per
+  // shot: its descriptor with the single-shot plan's chunk, its tensor
+  // maps, and its plan (tile items, or a segment list in d_sseg / d_sfirst).
+  int chains = -1;  // -1: chosen at the run (batch_auto_chains)
+  int last_chains = 0;  // the schedule of the last run
+  std::vector<ShotDesc> h_desc;
+  std::vector<ShotMaps> h_maps;
+  std::vector<ShotDesc> s_desc;
+  std::vector<int> s_nitems, s_grid;
+  std::vector<long> s_seg_off, s_first_off;  // s_seg_off < 0: tile items
+  int4 *d_sseg = nullptr;
+  int *d_sfirst = nullptr;
+  int splan_ctas = 0;
+  cudaStream_t chain_s[kMaxChains] = {};
+  cudaEvent_t fork = nullptr, join[kMaxChains] = {};
 };
 Batch B;
 
@@ -1530,6 +1547,11 @@ void batch_free_tables() {
   B.d_plan = nullptr;
   B.d_first = nullptr;
   B.plan_ctas = 0;
+  if (B.d_sseg) cudaFree(B.d_sseg);
+  if (B.d_sfirst) cudaFree(B.d_sfirst);
+  B.d_sseg = nullptr;
+  B.d_sfirst = nullptr;
+  B.splan_ctas = 0;
   if (B.d_desc) cudaFree(B.d_desc);
   if (B.d_maps) cudaFree(B.d_maps);
   if (B.d_items) cudaFree(B.d_items);
@@ -1559,6 +1581,11 @@ void batch_free() {
   }
   if (B.scratch) cudaFree(B.scratch);
   if (B.err_host) cudaFreeHost(B.err_host);
+  for (int c = 0; c < kMaxChains; ++c) {
+    if (B.chain_s[c]) cudaStreamDestroy(B.chain_s[c]);
+    if (B.join[c]) cudaEventDestroy(B.join[c]);
+  }
+  if (B.fork) cudaEventDestroy(B.fork);
   B = Batch();
 }
 
@@ -1629,6 +1656,8 @@ int batch_seal(int rows, int stages) {
   CK(cudaMemcpy(B.d_desc, desc.data(), sizeof(ShotDesc) * ns, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(B.d_maps, maps.data(), sizeof(ShotMaps) * ns, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(B.d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
+  B.h_desc = desc;
+  B.h_maps = maps;
   if (batch_half()) {
     CK(dev_malloc(&B.d_hshots, sizeof(HalfShot) * ns));
     CK(dev_malloc(&B.d_hmaps, sizeof(HalfShotMaps) * ns));
@@ -1693,6 +1722,68 @@ int batch_plan(int ctas) {
   CK(cudaMemcpy(B.d_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice));
   B.plan_ctas = ctas;
   return FLETCHER_OK;
+}
+
+// The chain schedule's per-shot plans for `ctas` persistent CTAs: each
+// shot's own single-shot plan, as DRIVER_Initialize would make it.
+int batch_single_plans(int ctas) {
+  if (B.splan_ctas == ctas && !B.s_desc.empty()) return FLETCHER_OK;
+  if (B.d_sseg) cudaFree(B.d_sseg);
+  if (B.d_sfirst) cudaFree(B.d_sfirst);
+  B.d_sseg = nullptr;
+  B.d_sfirst = nullptr;
+  const int ns = (int)B.shots.size();
+  B.s_desc.assign(ns, ShotDesc());
+  B.s_nitems.assign(ns, 0);
+  B.s_grid.assign(ns, 1);
+  B.s_seg_off.assign(ns, -1);
+  B.s_first_off.assign(ns, -1);
+  std::vector<int4> segs;
+  std::vector<int> firsts;
+  for (int i = 0; i < ns; ++i) {
+    const BatchShot &s = B.shots[i];
+    const int depth = s.sz - 2 * B.bord;
+    const Split sp = plan_segments(ctas, s.ntx, s.nty, B.sealed_rows, B.bord, depth, 0);
+    ShotDesc d = B.h_desc[i];
+    if (sp.spread) {
+      B.s_seg_off[i] = (long)segs.size();
+      B.s_first_off[i] = (long)firsts.size();
+      segs.insert(segs.end(), sp.seg.begin(), sp.seg.end());
+      firsts.insert(firsts.end(), sp.first.begin(), sp.first.end());
+      int grid = ctas;
+      while (grid > 1 && sp.first[grid - 1] == sp.first[grid]) --grid;
+      B.s_grid[i] = grid;
+      B.s_nitems[i] = (int)sp.seg.size();
+      d.chunk = 0;
+    } else {
+      d.chunk = sp.len;
+      B.s_nitems[i] = s.ntx * s.nty * ((depth + sp.len - 1) / sp.len);
+      B.s_grid[i] = std::min(B.s_nitems[i], ctas);
+    }
+    B.s_desc[i] = d;
+  }
+  if (!segs.empty()) {
+    CK(dev_malloc(&B.d_sseg, sizeof(int4) * segs.size()));
+    CK(dev_malloc(&B.d_sfirst, sizeof(int) * firsts.size()));
+    CK(cudaMemcpy(B.d_sseg, segs.data(), sizeof(int4) * segs.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(B.d_sfirst, firsts.data(), sizeof(int) * firsts.size(), cudaMemcpyHostToDevice));
+  }
+  B.splan_ctas = ctas;
+  return FLETCHER_OK;
+}
+
+// The schedule of an FP32 batch left to the library: one chain when most of
+// its work (updated cells x steps) is in shots that fill the GPU on their
+// own, else the persistent multi-shot launch.
+int batch_auto_chains(int steps) {
+  double fill = 0.0, total = 0.0;
+  for (const BatchShot &s : B.shots) {
+    const double cells = (double)(s.sx - 2 * B.bord) * (s.sy - 2 * B.bord) * (s.sz - 2 * B.bord);
+    const double work = cells * std::min(s.nsteps, steps);
+    total += work;
+    if (cells >= kChainFillCells) fill += work;
+  }
+  return 2.0 * fill >= total ? 1 : 0;
 }
 
 int batch_max_steps() {
@@ -1767,7 +1858,90 @@ int batch_issue(int it0, int it1, const float *src) {
   return FLETCHER_OK;
 }
 
+// The chain schedule: steps [0, steps) of every shot as single-shot
+// launches, the shots dealt (largest work first, to the least loaded chain)
+// over B.chains streams forked from and joined back into the library's
+// stream, so the whole run is one graph when captured.  A launch waits on
+// no other kernel, so kernels of different chains may share the GPU.
+int batch_issue_chains(int chains, int steps, const float *src) {
+  const int ns = (int)B.shots.size();
+  const int nc = std::max(1, std::min(std::min(chains, kMaxChains), ns));
+  if (!B.fork) CK(cudaEventCreateWithFlags(&B.fork, cudaEventDisableTiming));
+  for (int c = 0; c < nc; ++c) {
+    if (!B.chain_s[c]) CK(cudaStreamCreateWithFlags(&B.chain_s[c], cudaStreamNonBlocking));
+    if (!B.join[c]) CK(cudaEventCreateWithFlags(&B.join[c], cudaEventDisableTiming));
+  }
+  std::vector<std::vector<int>> chain(nc);
+  std::vector<double> load(nc, 0.0);
+  for (int oi = 0; oi < ns; ++oi) {
+    const int i = B.order[oi];
+    const BatchShot &s = B.shots[i];
+    const double work = (double)(s.sx - 2 * B.bord) * (s.sy - 2 * B.bord) * (s.sz - 2 * B.bord) *
+                        std::min(s.nsteps, steps);
+    const int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    chain[c].push_back(i);
+    load[c] += work;
+  }
+  PropLaunch L;
+  memset(&L, 0, sizeof(L));
+  L.batch = false;
+  L.tile_rows = B.sealed_rows;
+  L.stages = B.stages;
+  PropParams &P = L.p;
+  P.wait_ns = kWaitLimitNs;
+  P.stall_step = -1;
+  P.inv_dx = 1.0f / B.dx;
+  P.inv_dy = 1.0f / B.dy;
+  P.inv_dz = 1.0f / B.dz;
+  P.inv_dxx = 1.0f / (B.dx * B.dx);
+  P.inv_dyy = 1.0f / (B.dy * B.dy);
+  P.inv_dzz = 1.0f / (B.dz * B.dz);
+  P.inv_dxy = 1.0f / (B.dx * B.dy);
+  P.inv_dxz = 1.0f / (B.dx * B.dz);
+  P.inv_dyz = 1.0f / (B.dy * B.dz);
+  P.iso = (B.dx == B.dy && B.dx == B.dz) ? 1 : 0;
+  P.dt2 = P.iso ? (B.dt * B.dt) * P.inv_dxx : B.dt * B.dt;
+  P.dt = B.dt;
+  P.err = B.err_dev;
+  CK(cudaEventRecord(B.fork, g_stream));
+  for (int c = 0; c < nc; ++c) {
+    cudaStream_t cs = B.chain_s[c];
+    CK(cudaStreamWaitEvent(cs, B.fork, 0));
+    for (const int i : chain[c]) {
+      const ShotMaps &m = B.h_maps[i];
+      P.one = B.s_desc[i];
+      P.nitems = B.s_nitems[i];
+      P.seg = B.s_seg_off[i] < 0 ? nullptr : B.d_sseg + B.s_seg_off[i];
+      P.cta_first = B.s_seg_off[i] < 0 ? nullptr : B.d_sfirst + B.s_first_off[i];
+      L.grid = B.s_grid[i];
+      L.m.arr = m.arr;
+      L.m.upd = m.upd;
+      const int n = std::min(B.shots[i].nsteps, steps);
+      for (int it = 0; it < n; ++it) {
+        P.parity = it & 1;
+        P.src = src[it];
+        P.cor = it > 0 ? src[it - 1] : 0.0f;
+        L.m.cur_halo = m.halo[P.parity];
+        L.m.prev_pt = m.pt[P.parity ^ 1];
+        CK(propagate_fp32_launch(L, cs));
+        ++B.launches;
+      }
+    }
+    CK(cudaEventRecord(B.join[c], cs));
+    CK(cudaStreamWaitEvent(g_stream, B.join[c], 0));
+  }
+  return FLETCHER_OK;
+}
+
 }  // namespace
+
+extern "C" int FLETCHER_BatchSetChains(int chains) {
+  if (chains < -1 || chains > kMaxChains)
+    return fail(FLETCHER_ERR_ARGS, "FLETCHER_BatchSetChains: chains must be -1 .. %d (got %d)", kMaxChains, chains);
+  if (!B.open) return fail(FLETCHER_ERR_ARGS, "FLETCHER_BatchSetChains before FLETCHER_BatchCreate");
+  B.chains = chains;
+  return FLETCHER_OK;
+}
 
 extern "C" int FLETCHER_BatchCreate(int bord, float dx, float dy, float dz, float dt) {
   batch_free();
@@ -1923,7 +2097,11 @@ extern "C" int FLETCHER_BatchRun(const float *src, int max_steps, int use_graph,
   if (per_sm < 1)
     return fail(FLETCHER_ERR_CUDA, "tile shape (%d rows, %d stages) fits no CTA on an SM", B.sealed_rows, B.stages);
   B.ctas = B.num_sms * per_sm;
-  if (!batch_half() && batch_plan(B.ctas)) return g_last_err;
+  const int nchains = batch_half() ? 0 : (B.chains < 0 ? batch_auto_chains(steps) : B.chains);
+  B.last_chains = nchains;
+  const bool chains = nchains > 0;
+  if (chains ? batch_single_plans(B.ctas) : (!batch_half() && batch_plan(B.ctas))) return g_last_err;
+  auto issue = [&]() { return chains ? batch_issue_chains(nchains, steps, src) : batch_issue(0, steps, src); };
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -1931,7 +2109,7 @@ extern "C" int FLETCHER_BatchRun(const float *src, int max_steps, int use_graph,
   if (use_graph) {
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(g_stream, cudaStreamCaptureModeThreadLocal));
-    const int rc = batch_issue(0, steps, src);
+    const int rc = issue();
     cudaError_t ce = cudaStreamEndCapture(g_stream, &graph);
     if (rc) return rc;
     CK(ce);
@@ -1942,7 +2120,7 @@ extern "C" int FLETCHER_BatchRun(const float *src, int max_steps, int use_graph,
   CK(cudaEventRecord(e0, g_stream));
   if (use_graph) {
     CK(cudaGraphLaunch(exec, g_stream));
-  } else if (batch_issue(0, steps, src)) {
+  } else if (issue()) {
     return g_last_err;
   }
   CK(cudaEventRecord(e1, g_stream));
@@ -1995,6 +2173,8 @@ extern "C" int FLETCHER_BatchSetTileConfig(int rows, int stages) {
   B.stages = s;
   return FLETCHER_OK;
 }
+
+extern "C" int FLETCHER_BatchLastChains(void) { return B.last_chains; }
 
 extern "C" int FLETCHER_BatchInfo(long *nshots, double *cell_steps, long *launches, size_t *device_bytes) {
   if (nshots) *nshots = (long)B.shots.size();

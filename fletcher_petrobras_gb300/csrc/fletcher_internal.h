@@ -114,6 +114,13 @@ cudaError_t propagate_fp32_prepare(int tile_rows, int stages);
 cudaError_t propagate_fp32_launch(const PropLaunch &L, cudaStream_t s);
 // Tile shape of the Der1-Der1 numerics (the only one built for it).
 constexpr int kD1D1Rows = 16, kD1D1Stages = 4;
+// Most concurrent chains of the batched shots' chain schedule, and the
+// updated cells from which a shot fills the GPU on its own (measured on
+// GB300: at 2.1 M cells a chain and the persistent launch tie; below, the
+// persistent launch is 6-7% faster; at 4.7 M cells and more one chain is
+// 7% faster).
+constexpr int kMaxChains = 8;
+constexpr double kChainFillCells = 2.1e6;
 
 // ---- 16-bit field storage (propagate_half.cu) ----
 // A field buffer holds (p, q) as half2 per cell ([z][y][pitch]) and, in the

@@ -110,11 +110,11 @@ def test_half_batch_matches_single_shot_runs(form):
 
 @pytest.mark.parametrize("form", ["fp32", "fp16x"])
 def test_batch_with_three_spacings_matches_single_shot_runs(form, orc):
-    """dx, dy, dz all different (the kernels' non-isotropic path).  There the
-    last bits of a cell depend on how its tile column is split in z (whole
-    columns, as the batch runs them, or the single-shot plan's segments), so
-    batched shots are compared with their single-shot runs to 1e-6 and with
-    the oracle to 1e-5 rather than bit for bit."""
+    """dx, dy, dz all different (the kernels' non-isotropic path): the rings
+    and the exchange hold unscaled first derivatives and each cross
+    derivative takes one combined factor, so a cell's floats do not depend
+    on how its tile column is split in z -- batched shots equal their
+    single-shot runs bit for bit, and the oracle bounds them."""
     sp = dict(dx=10.0, dy=12.5, dz=15.0, dt=0.0005)
     shots = [s.with_(**sp) for s in SHOTS[:2]]
     models = [p.model() for p in shots]
@@ -127,7 +127,7 @@ def test_batch_with_three_spacings_matches_single_shot_runs(form, orc):
     for i, (p, m) in enumerate(zip(shots, models)):
         ref = single(p, m, form)
         for k in range(4):
-            assert rel_l2(got[i][k], ref[k]) < 1e-6, (form, i, k)
+            assert np.array_equal(got[i][k], ref[k]), (form, i, k, rel_l2(got[i][k], ref[k]))
         op, oq, _, _ = orc.run_f32(p, m)
         tol = 1e-5 if form == "fp32" else 1e-4
         assert rel_l2(got[i][0], op) < tol and rel_l2(got[i][1], oq) < tol
@@ -155,3 +155,42 @@ def test_deep_shots_split_in_z_match_single_shot_runs(form):
         assert np.abs(ref[0]).max() > 0.0
         for k in range(4):
             assert np.array_equal(got[i][k], ref[k]), (form, i, k)
+
+
+@pytest.mark.parametrize("chains", [1, 2, 3])
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_chain_schedule_matches_single_shot_runs(chains, use_graph):
+    """FLETCHER_BatchSetChains: each shot's steps as single-shot launches on
+    one of `chains` concurrent streams.  Shots whose plans share out their
+    last round (segment lists) and shots on round-robin chunks (tile items),
+    three spacings included: every shot equals its own single-shot run."""
+    shots = SHOTS + [
+        Problem("c3", 70, 60, 150, absorb=5, dt=0.0006, steps=13, fcut=45.0, kind="layered", layers=4, seed=33,
+                source=(35, 30, 70)),
+        SHOTS[0].with_(name="c4", dx=10.0, dy=12.5, dz=15.0, dt=0.0005),
+    ]
+    models = [p.model() for p in shots]
+    batch = Batch(chains=chains, dx=12.5, dy=12.5, dz=12.5)
+    for p, m in zip(shots[:-1], models[:-1]):
+        batch.add(p, m)
+    batch.run(use_graph=use_graph)
+    got = [[batch.field(i, k) for k in range(4)] for i in range(len(shots) - 1)]
+    info = batch.info()
+    batch.close()
+    assert info["launches"] == sum(p.steps for p in shots[:-1])
+    for i, (p, m) in enumerate(zip(shots[:-1], models[:-1])):
+        ref = single(p, m)
+        assert np.abs(ref[0]).max() > 0.0
+        for k in range(4):
+            assert np.array_equal(got[i][k], ref[k]), (chains, i, k)
+    # A three-spacing batch on the chain schedule.
+    p, m = shots[-1], models[-1]
+    batch = Batch(chains=chains, dx=p.dx, dy=p.dy, dz=p.dz, dt=p.dt)
+    batch.add(p, m)
+    batch.run(use_graph=use_graph)
+    got = [batch.field(0, k) for k in range(4)]
+    batch.close()
+    ref = single(p, m)
+    for k in range(4):
+        assert np.array_equal(got[k], ref[k]), (chains, "three spacings", k)
+

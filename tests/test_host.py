@@ -115,6 +115,19 @@ def test_argument_errors_are_reported_not_fatal(lib):
     assert lib.FLETCHER_SetTileConfig(7, 4, 0) == 1  # shape not built
     lib.FLETCHER_ClearError()
     assert lib.FLETCHER_SetTileConfig(0, 0, 0) == 0
+    assert lib.FLETCHER_SetCoefLayout(3) == 1
+    assert b"coefficient layout" in lib.FLETCHER_GetLastErrorString()
+    lib.FLETCHER_ClearError()
+    assert lib.FLETCHER_SetCoefLayout(1) == 0
+    assert lib.FLETCHER_CoefLayout() < 0  # not initialised
+    lib.FLETCHER_ClearError()
+    assert lib.FLETCHER_BatchSetChains(9) == 1
+    assert b"chains must be -1" in lib.FLETCHER_GetLastErrorString()
+    lib.FLETCHER_ClearError()
+    assert lib.FLETCHER_BatchSetChains(2) == 1  # no batch open
+    lib.FLETCHER_ClearError()
+    ph = (ctypes.c_double * 5)()
+    assert lib.FLETCHER_InitPhases(ph) == 0
 
 
 @pytest.mark.skipif(reference_dir() is None, reason="reference sources absent (FLETCHER_REF_DIR or staged copy)")
