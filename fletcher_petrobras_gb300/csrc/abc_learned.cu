@@ -38,7 +38,10 @@
 //     after the plain step that also applies the one-way update): one warp
 //     evaluates 16 ghost cells, the layer-1 and layer-2 outputs stay in
 //     registers as the next layer's A fragments, and k stays in registers
-//     until the update uses it;
+//     until the update uses it; the weights' B fragments are read from a
+//     shared-memory copy (in registers they took 62 of 128, and the SM held
+//     16 warps instead of 24: 119 against 90 us per evaluating step at
+//     256^3);
 //   * training (k_abc_train) is a per-sample forward and backward pass in
 //     FP32 with the same roundings (straight-through), block sums of the
 //     gradients added up in block order (k_abc_reduce: training is
@@ -535,6 +538,94 @@ __device__ __forceinline__ void mlp16(const __half *Xs, const Frags &F, float (&
   y_hi[1] = o[3];
 }
 
+// The same fragments in shared memory, lane-minor (word [..][lane]: a
+// warp's 32 lanes read 32 consecutive words, no bank conflict), for the
+// boundary kernel: there the 62 registers of Frags would hold the SM to 16
+// warps.
+struct FragsSmem {
+  uint32_t w1[4][3][2][32];
+  uint32_t w2[4][2][2][32];
+  uint32_t w3[2][2][32];
+  float b1[4][2][32], b2[4][2][32], b3[2][32];
+};
+
+// Fills S from the network, warp 0 writing its lanes' fragments.
+__device__ __forceinline__ void frags_to_smem(const NetHalf *__restrict__ N, FragsSmem &S) {
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  Frags F;
+  load_frags(N, F);
+#pragma unroll
+  for (int nt = 0; nt < 4; ++nt) {
+#pragma unroll
+    for (int ks = 0; ks < 3; ++ks)
+      for (int h = 0; h < 2; ++h) S.w1[nt][ks][h][lane] = F.w1[nt][ks][h];
+#pragma unroll
+    for (int kt = 0; kt < 2; ++kt)
+      for (int h = 0; h < 2; ++h) S.w2[nt][kt][h][lane] = F.w2[nt][kt][h];
+    for (int h = 0; h < 2; ++h) {
+      S.b1[nt][h][lane] = F.b1[nt][h];
+      S.b2[nt][h][lane] = F.b2[nt][h];
+    }
+  }
+#pragma unroll
+  for (int kt = 0; kt < 2; ++kt)
+    for (int h = 0; h < 2; ++h) S.w3[kt][h][lane] = F.w3[kt][h];
+  for (int h = 0; h < 2; ++h) S.b3[h][lane] = F.b3[h];
+}
+
+// mlp16 with the B fragments and biases read from shared memory.
+__device__ __forceinline__ void mlp16_smem(const __half *Xs, const FragsSmem &S, float (&y_lo)[2],
+                                           float (&y_hi)[2]) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  uint32_t a[3][4];
+#pragma unroll
+  for (int ks = 0; ks < 3; ++ks) {
+    a[ks][0] = *reinterpret_cast<const uint32_t *>(Xs + g * kXs + 16 * ks + 2 * t);
+    a[ks][1] = *reinterpret_cast<const uint32_t *>(Xs + (g + 8) * kXs + 16 * ks + 2 * t);
+    a[ks][2] = *reinterpret_cast<const uint32_t *>(Xs + g * kXs + 16 * ks + 2 * t + 8);
+    a[ks][3] = *reinterpret_cast<const uint32_t *>(Xs + (g + 8) * kXs + 16 * ks + 2 * t + 8);
+  }
+  float h[4][4];
+#pragma unroll
+  for (int nt = 0; nt < 4; ++nt) {
+    const float c0 = S.b1[nt][0][lane], c1 = S.b1[nt][1][lane];
+    h[nt][0] = c0; h[nt][1] = c1; h[nt][2] = c0; h[nt][3] = c1;
+#pragma unroll
+    for (int ks = 0; ks < 3; ++ks) mma16816(h[nt], a[ks], S.w1[nt][ks][0][lane], S.w1[nt][ks][1][lane]);
+  }
+  uint32_t a2[2][4];
+#pragma unroll
+  for (int kt = 0; kt < 2; ++kt) {
+    a2[kt][0] = tanh_h2(h[2 * kt][0], h[2 * kt][1]);
+    a2[kt][1] = tanh_h2(h[2 * kt][2], h[2 * kt][3]);
+    a2[kt][2] = tanh_h2(h[2 * kt + 1][0], h[2 * kt + 1][1]);
+    a2[kt][3] = tanh_h2(h[2 * kt + 1][2], h[2 * kt + 1][3]);
+  }
+#pragma unroll
+  for (int nt = 0; nt < 4; ++nt) {
+    const float c0 = S.b2[nt][0][lane], c1 = S.b2[nt][1][lane];
+    h[nt][0] = c0; h[nt][1] = c1; h[nt][2] = c0; h[nt][3] = c1;
+#pragma unroll
+    for (int kt = 0; kt < 2; ++kt) mma16816(h[nt], a2[kt], S.w2[nt][kt][0][lane], S.w2[nt][kt][1][lane]);
+  }
+#pragma unroll
+  for (int kt = 0; kt < 2; ++kt) {
+    a2[kt][0] = tanh_h2(h[2 * kt][0], h[2 * kt][1]);
+    a2[kt][1] = tanh_h2(h[2 * kt][2], h[2 * kt][3]);
+    a2[kt][2] = tanh_h2(h[2 * kt + 1][0], h[2 * kt + 1][1]);
+    a2[kt][3] = tanh_h2(h[2 * kt + 1][2], h[2 * kt + 1][3]);
+  }
+  const float o0 = S.b3[0][lane], o1 = S.b3[1][lane];
+  float o[4] = {o0, o1, o0, o1};
+#pragma unroll
+  for (int kt = 0; kt < 2; ++kt) mma16816(o, a2[kt], S.w3[kt][0][lane], S.w3[kt][1][lane]);
+  y_lo[0] = o[0];
+  y_lo[1] = o[1];
+  y_hi[0] = o[2];
+  y_hi[1] = o[3];
+}
+
 constexpr int kInferWarps = 8;
 
 __device__ __forceinline__ float sigmoid(float y) { return 1.0f / (1.0f + __expf(-y)); }
@@ -615,6 +706,7 @@ struct BoundaryArgs {
 };
 
 constexpr int kBoundaryWarps = 8;
+constexpr int kBoundaryBlocks = 3;  // resident blocks of the network kernel per SM (at most 85 registers)
 
 // Field index of cell d = L-3+j of ray `ray` of the face pair normal to axis
 // A (rays [r0, rmid) on the low face, [rmid, ...) on the high one, each face
@@ -670,13 +762,14 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks, ui
   return ok_s != 0;
 }
 
-__global__ void __launch_bounds__(32 * kBoundaryWarps, 2) k_abc_boundary(const __grid_constant__ BoundaryArgs B) {
+__global__ void __launch_bounds__(32 * kBoundaryWarps, kBoundaryBlocks) k_abc_boundary(const __grid_constant__ BoundaryArgs B) {
   __shared__ __align__(16) __half Xs[kBoundaryWarps][16 * kXs];
   __shared__ float2 Ln[kBoundaryWarps][2][4][8];  // [time: t, t-1][ray][point] (p, q)
+  __shared__ FragsSmem F;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const Ghost &G = B.G;
-  Frags F;
-  load_frags(B.net, F);
+  frags_to_smem(B.net, F);
+  __syncthreads();
   const long wg = (long)blockIdx.x * kBoundaryWarps + warp, nw = (long)gridDim.x * kBoundaryWarps;
   for (int A = 2; A >= 0; --A) {
     const int fa = 2 * (2 - A);                       // the low face; fa + 1 is the high one
@@ -759,7 +852,7 @@ __global__ void __launch_bounds__(32 * kBoundaryWarps, 2) k_abc_boundary(const _
         }
         __syncwarp();
         float ylo[2], yhi[2];
-        mlp16(X, F, ylo, yhi);
+        mlp16_smem(X, F, ylo, yhi);
         // Rows g and g + 8 sit in lane 4 g: cell u comes from lane 4 (u % 8).
         const int src = 4 * (u & 7);
         const float a0 = __shfl_sync(0xffffffffu, ylo[0], src), a1 = __shfl_sync(0xffffffffu, ylo[1], src);
