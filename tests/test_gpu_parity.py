@@ -304,3 +304,33 @@ def test_host_access_and_copy_paths_identical():
     assert modes[1] == 0
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("stop", [1, 13])
+def test_checkpoint_and_resume_bit_identical(stop):
+    """Checkpoint / resume: the four fields read back after `stop` steps
+    (FLETCHER_GetField: current and previous p and q, as the reference's
+    arrays hold them, the last step's source included) are the initial state
+    of a new DRIVER_Initialize, and the run continues with the source of step
+    stop + 1 on.  The FP32 result equals the uninterrupted run's bit for bit."""
+    prob = Problem("ckpt", 30, 26, 22, absorb=4, dt=0.0006, steps=24, fcut=45.0, kind="layered", layers=3, seed=5)
+    m = prob.model()
+    src = prob.sources()
+    full = gpu_run(prob, m)
+    prop = Propagator()
+    prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, m)
+    for it in range(1, stop + 1):
+        prop.insert_source(it - 1, prob.i_source, src[it - 1])
+        prop.propagate(it)
+    pc, qc, pp, qp = (prop.field(k) for k in range(4))
+    prop.finalize()
+    prop = Propagator()
+    prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, m,
+                    pp=pp, pc=pc, qp=qp, qc=qc)
+    for it in range(stop + 1, prob.steps + 1):
+        prop.insert_source(it - 1, prob.i_source, src[it - 1])
+        prop.propagate(it)
+    resumed = [prop.field(k) for k in range(4)]
+    prop.finalize()
+    for a, b in zip(resumed, full):
+        assert np.array_equal(a, b), rel_l2(a, b)
