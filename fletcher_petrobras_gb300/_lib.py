@@ -30,6 +30,7 @@ SIGNATURES = {
     "FLETCHER_SetCoefLayout": (C.c_int, [C.c_int]),
     "FLETCHER_CoefLayout": (C.c_int, []),
     "FLETCHER_InitPhases": (C.c_int, [DP]),
+    "FLETCHER_DebugPoisonPadding": (C.c_int, [C.c_float]),
     "FLETCHER_InjectFault": (C.c_int, [C.c_int, C.c_int, C.c_int]),
     "FLETCHER_SetHostAccess": (C.c_int, [C.c_int]),
     "FLETCHER_HostAccess": (C.c_int, []),

@@ -349,6 +349,17 @@ __global__ void k_unpack_coef(const float *__restrict__ coef, float *__restrict_
   }
 }
 
+// Test aid: writes v into the pitch padding (columns sx .. pitch-1) of
+// `rows` rows of `width` floats per cell.
+__global__ void k_poison_pad(float *buf, int width, int sx, int pitch, long rows, float v) {
+  const long pad = (long)(pitch - sx) * width;
+  const long n = rows * pad;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const long r = i / pad, c = i % pad;
+    buf[r * (long)pitch * width + (long)sx * width + c] = v;
+  }
+}
+
 // Adds val to both fields of one cell (source outside the fused path).
 __global__ void k_add_source(float2 *F, size_t idx, float val) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
@@ -1250,6 +1261,23 @@ extern "C" int FLETCHER_SetForm(int form) {
   if (form < FLETCHER_FORM_FP32 || form > FLETCHER_FORM_FP16X)
     return fail(FLETCHER_ERR_ARGS, "unknown storage form %d", form);
   g_form = form;
+  return FLETCHER_OK;
+}
+
+extern "C" int FLETCHER_DebugPoisonPadding(float v) {
+  if (!g.init) return fail(FLETCHER_ERR_ARGS, "FLETCHER_DebugPoisonPadding before DRIVER_Initialize");
+  if (half_form()) return fail(FLETCHER_ERR_ARGS, "FLETCHER_DebugPoisonPadding: FP32 form only");
+  if (g.pitch == g.sx) return FLETCHER_OK;  // no padding
+  const long rows = (long)g.sy * g.sz;
+  for (int b = 0; b < 2; ++b) {
+    k_poison_pad<<<grid_for((size_t)rows * (g.pitch - g.sx) * 2), 256, 0, g_stream>>>(
+        reinterpret_cast<float *>(g.F[b]), 2, g.sx, g.pitch, rows, v);
+    CK(cudaGetLastError());
+  }
+  k_poison_pad<<<grid_for((size_t)rows * kNumCoef * (g.pitch - g.sx)), 256, 0, g_stream>>>(
+      g.coef, 1, g.sx, g.pitch, rows * kNumCoef, v);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(g_stream));
   return FLETCHER_OK;
 }
 

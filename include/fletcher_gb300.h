@@ -238,6 +238,12 @@ int FLETCHER_GetCoefficients(float *host);
 /* Number of propagate-kernel launches issued since DRIVER_Initialize. */
 long FLETCHER_KernelLaunches(void);
 
+/* Test aid, in place of a memory sanitizer: writes v into the pitch padding
+ * (columns sx .. pitch-1 of every row) of both field buffers and of the
+ * coefficient block of the initialised FP32 state.  Those cells are never
+ * read, so NaN there must leave every result unchanged. */
+int FLETCHER_DebugPoisonPadding(float v);
+
 /* Wall-clock phases (s) of the last successful DRIVER_Initialize, in out[5]:
  * device allocations; locking the caller's host arrays and issuing their
  * copies; the device work (copies, coefficient precompute, field packing)

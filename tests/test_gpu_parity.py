@@ -334,3 +334,29 @@ def test_checkpoint_and_resume_bit_identical(stop):
     prop.finalize()
     for a, b in zip(resumed, full):
         assert np.array_equal(a, b), rel_l2(a, b)
+
+
+@pytest.mark.parametrize("kw", [{}, {"numerics": "d1d1"}, {"coef_layout": "media"}, {"tile_rows": 12, "stages": 5}])
+def test_pitch_padding_is_never_read(kw):
+    """NaN written into the pitch padding of the field buffers and the
+    coefficient block (columns sx .. pitch-1, FLETCHER_DebugPoisonPadding)
+    changes no result: the kernels read only the grid's own cells."""
+    prob = Problem("pad", 37, 21, 15, absorb=4, dt=0.0006, steps=18, fcut=45.0, kind="layered", layers=3, seed=7)
+    assert prob.sx % 32 != 0
+    m = prob.model()
+    src = prob.sources()
+    out = []
+    for poison in (False, True):
+        prop = Propagator(**kw)
+        prop.initialize(prob.sx, prob.sy, prob.sz, prob.bord, prob.dx, prob.dy, prob.dz, prob.dt, m)
+        if poison:
+            assert prop.lib.FLETCHER_DebugPoisonPadding(float("nan")) == 0
+        for it in range(1, prob.steps + 1):
+            prop.insert_source(it - 1, prob.i_source, src[it - 1])
+            prop.propagate(it)
+        out.append([prop.field(k) for k in range(4)])
+        prop.finalize()
+    Propagator()
+    for a, b in zip(*out):
+        assert np.isfinite(b).all()
+        assert np.array_equal(a, b)
