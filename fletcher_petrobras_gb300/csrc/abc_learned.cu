@@ -538,15 +538,16 @@ __device__ __forceinline__ void mlp16(const __half *Xs, const Frags &F, float (&
   y_hi[1] = o[3];
 }
 
-// The same fragments in shared memory, lane-minor (word [..][lane]: a
-// warp's 32 lanes read 32 consecutive words, no bank conflict), for the
-// boundary kernel: there the 62 registers of Frags would hold the SM to 16
-// warps.
+// The same fragments in shared memory, lane-minor with a lane's two words
+// side by side ([..][lane][2]: one 8-byte load per MMA operand or bias
+// pair, a warp's 32 lanes reading 256 consecutive bytes, no bank conflict),
+// for the boundary kernel: there the 62 registers of Frags would hold the
+// SM to 16 warps.
 struct FragsSmem {
-  uint32_t w1[4][3][2][32];
-  uint32_t w2[4][2][2][32];
-  uint32_t w3[2][2][32];
-  float b1[4][2][32], b2[4][2][32], b3[2][32];
+  uint2 w1[4][3][32];
+  uint2 w2[4][2][32];
+  uint2 w3[2][32];
+  float2 b1[4][32], b2[4][32], b3[32];
 };
 
 // Fills S from the network, warp 0 writing its lanes' fragments.
@@ -558,20 +559,15 @@ __device__ __forceinline__ void frags_to_smem(const NetHalf *__restrict__ N, Fra
 #pragma unroll
   for (int nt = 0; nt < 4; ++nt) {
 #pragma unroll
-    for (int ks = 0; ks < 3; ++ks)
-      for (int h = 0; h < 2; ++h) S.w1[nt][ks][h][lane] = F.w1[nt][ks][h];
+    for (int ks = 0; ks < 3; ++ks) S.w1[nt][ks][lane] = make_uint2(F.w1[nt][ks][0], F.w1[nt][ks][1]);
 #pragma unroll
-    for (int kt = 0; kt < 2; ++kt)
-      for (int h = 0; h < 2; ++h) S.w2[nt][kt][h][lane] = F.w2[nt][kt][h];
-    for (int h = 0; h < 2; ++h) {
-      S.b1[nt][h][lane] = F.b1[nt][h];
-      S.b2[nt][h][lane] = F.b2[nt][h];
-    }
+    for (int kt = 0; kt < 2; ++kt) S.w2[nt][kt][lane] = make_uint2(F.w2[nt][kt][0], F.w2[nt][kt][1]);
+    S.b1[nt][lane] = make_float2(F.b1[nt][0], F.b1[nt][1]);
+    S.b2[nt][lane] = make_float2(F.b2[nt][0], F.b2[nt][1]);
   }
 #pragma unroll
-  for (int kt = 0; kt < 2; ++kt)
-    for (int h = 0; h < 2; ++h) S.w3[kt][h][lane] = F.w3[kt][h];
-  for (int h = 0; h < 2; ++h) S.b3[h][lane] = F.b3[h];
+  for (int kt = 0; kt < 2; ++kt) S.w3[kt][lane] = make_uint2(F.w3[kt][0], F.w3[kt][1]);
+  S.b3[lane] = make_float2(F.b3[0], F.b3[1]);
 }
 
 // mlp16 with the B fragments and biases read from shared memory.
@@ -589,10 +585,13 @@ __device__ __forceinline__ void mlp16_smem(const __half *Xs, const FragsSmem &S,
   float h[4][4];
 #pragma unroll
   for (int nt = 0; nt < 4; ++nt) {
-    const float c0 = S.b1[nt][0][lane], c1 = S.b1[nt][1][lane];
-    h[nt][0] = c0; h[nt][1] = c1; h[nt][2] = c0; h[nt][3] = c1;
+    const float2 c = S.b1[nt][lane];
+    h[nt][0] = c.x; h[nt][1] = c.y; h[nt][2] = c.x; h[nt][3] = c.y;
 #pragma unroll
-    for (int ks = 0; ks < 3; ++ks) mma16816(h[nt], a[ks], S.w1[nt][ks][0][lane], S.w1[nt][ks][1][lane]);
+    for (int ks = 0; ks < 3; ++ks) {
+      const uint2 w = S.w1[nt][ks][lane];
+      mma16816(h[nt], a[ks], w.x, w.y);
+    }
   }
   uint32_t a2[2][4];
 #pragma unroll
@@ -604,10 +603,13 @@ __device__ __forceinline__ void mlp16_smem(const __half *Xs, const FragsSmem &S,
   }
 #pragma unroll
   for (int nt = 0; nt < 4; ++nt) {
-    const float c0 = S.b2[nt][0][lane], c1 = S.b2[nt][1][lane];
-    h[nt][0] = c0; h[nt][1] = c1; h[nt][2] = c0; h[nt][3] = c1;
+    const float2 c = S.b2[nt][lane];
+    h[nt][0] = c.x; h[nt][1] = c.y; h[nt][2] = c.x; h[nt][3] = c.y;
 #pragma unroll
-    for (int kt = 0; kt < 2; ++kt) mma16816(h[nt], a2[kt], S.w2[nt][kt][0][lane], S.w2[nt][kt][1][lane]);
+    for (int kt = 0; kt < 2; ++kt) {
+      const uint2 w = S.w2[nt][kt][lane];
+      mma16816(h[nt], a2[kt], w.x, w.y);
+    }
   }
 #pragma unroll
   for (int kt = 0; kt < 2; ++kt) {
@@ -616,10 +618,13 @@ __device__ __forceinline__ void mlp16_smem(const __half *Xs, const FragsSmem &S,
     a2[kt][2] = tanh_h2(h[2 * kt + 1][0], h[2 * kt + 1][1]);
     a2[kt][3] = tanh_h2(h[2 * kt + 1][2], h[2 * kt + 1][3]);
   }
-  const float o0 = S.b3[0][lane], o1 = S.b3[1][lane];
-  float o[4] = {o0, o1, o0, o1};
+  const float2 ob = S.b3[lane];
+  float o[4] = {ob.x, ob.y, ob.x, ob.y};
 #pragma unroll
-  for (int kt = 0; kt < 2; ++kt) mma16816(o, a2[kt], S.w3[kt][0][lane], S.w3[kt][1][lane]);
+  for (int kt = 0; kt < 2; ++kt) {
+    const uint2 w = S.w3[kt][lane];
+    mma16816(o, a2[kt], w.x, w.y);
+  }
   y_lo[0] = o[0];
   y_lo[1] = o[1];
   y_hi[0] = o[2];
