@@ -194,3 +194,26 @@ def test_chain_schedule_matches_single_shot_runs(chains, use_graph):
     for k in range(4):
         assert np.array_equal(got[k], ref[k]), (chains, "three spacings", k)
 
+
+
+def test_default_schedule_follows_shot_size():
+    """FLETCHER_BatchSetChains(-1), the default: small shots share the
+    persistent launch; a batch whose work is mostly in shots of at least
+    2.1 M updated cells (they fill the GPU on their own) runs one chain.
+    Both give each shot its single-shot fields."""
+    small = SHOTS[:2]
+    big = Problem("big", 136, 120, 128, absorb=4, dt=0.0006, steps=6, fcut=45.0, kind="layered", layers=3, seed=41,
+                  source=(70, 64, 60))
+    assert (big.sx - 8) * (big.sy - 8) * (big.sz - 8) >= 2.1e6
+    for shots, want in ((small, 0), ([big] + small, 1)):
+        models = [p.model() for p in shots]
+        batch = Batch()
+        for p, m in zip(shots, models):
+            batch.add(p, m)
+        batch.run()
+        got = [batch.field(i, 0) for i in range(len(shots))]
+        chains = batch.info()["chains"]
+        batch.close()
+        assert chains == want
+        for i, (p, m) in enumerate(zip(shots, models)):
+            assert np.array_equal(got[i], single(p, m)[0]), (want, i)
