@@ -1558,6 +1558,8 @@ struct Batch {
   int last_chains = 0;  // the schedule of the last run
   std::vector<ShotDesc> h_desc;
   std::vector<ShotMaps> h_maps;
+  std::vector<HalfShot> h_hshots;   // 16-bit forms
+  std::vector<HalfShotMaps> h_hmaps;
   std::vector<ShotDesc> s_desc;
   std::vector<int> s_nitems, s_grid;
   std::vector<long> s_seg_off, s_first_off;  // s_seg_off < 0: tile items
@@ -1686,6 +1688,8 @@ int batch_seal(int rows, int stages) {
   CK(cudaMemcpy(B.d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
   B.h_desc = desc;
   B.h_maps = maps;
+  B.h_hshots = hshots;
+  B.h_hmaps = hmaps;
   if (batch_half()) {
     CK(dev_malloc(&B.d_hshots, sizeof(HalfShot) * ns));
     CK(dev_malloc(&B.d_hmaps, sizeof(HalfShotMaps) * ns));
@@ -1753,7 +1757,8 @@ int batch_plan(int ctas) {
 }
 
 // The chain schedule's per-shot plans for `ctas` persistent CTAs: each
-// shot's own single-shot plan, as DRIVER_Initialize would make it.
+// shot's own single-shot plan, as DRIVER_Initialize would make it (the
+// 16-bit kernel always walks a segment list).
 int batch_single_plans(int ctas) {
   if (B.splan_ctas == ctas && !B.s_desc.empty()) return FLETCHER_OK;
   if (B.d_sseg) cudaFree(B.d_sseg);
@@ -1773,7 +1778,7 @@ int batch_single_plans(int ctas) {
     const int depth = s.sz - 2 * B.bord;
     const Split sp = plan_segments(ctas, s.ntx, s.nty, B.sealed_rows, B.bord, depth, 0);
     ShotDesc d = B.h_desc[i];
-    if (sp.spread) {
+    if (sp.spread || batch_half()) {
       B.s_seg_off[i] = (long)segs.size();
       B.s_first_off[i] = (long)firsts.size();
       segs.insert(segs.end(), sp.seg.begin(), sp.seg.end());
@@ -1931,11 +1936,50 @@ int batch_issue_chains(int chains, int steps, const float *src) {
   P.dt2 = P.iso ? (B.dt * B.dt) * P.inv_dxx : B.dt * B.dt;
   P.dt = B.dt;
   P.err = B.err_dev;
+  const bool half = batch_half(), ext = B.form == FLETCHER_FORM_FP16X;
   CK(cudaEventRecord(B.fork, g_stream));
   for (int c = 0; c < nc; ++c) {
     cudaStream_t cs = B.chain_s[c];
     CK(cudaStreamWaitEvent(cs, B.fork, 0));
     for (const int i : chain[c]) {
+      if (half) {
+        // The single-shot 16-bit step: the new planes' scales, then the
+        // step (buffer it & 1 current, exponent slot it % 3, as the
+        // persistent launch keeps them).
+        const HalfShot &h = B.h_hshots[i];
+        const int sz = B.shots[i].sz;
+        HalfLaunch HL;
+        memset(&HL, 0, sizeof(HL));
+        HL.batch = false;
+        HL.h.p = P;
+        HL.h.p.one = B.s_desc[i];
+        HL.h.p.nitems = B.s_nitems[i];
+        HL.h.p.seg = B.d_sseg + B.s_seg_off[i];
+        HL.h.p.cta_first = B.d_sfirst + B.s_first_off[i];
+        HL.tile_rows = B.sealed_rows;
+        HL.stages = B.stages;
+        HL.grid = B.s_grid[i];
+        const int n = std::min(B.shots[i].nsteps, steps);
+        for (int it = 0; it < n; ++it) {
+          const int cur = it & 1, prv = cur ^ 1;
+          const int ecur = it % 3, enew = (it + 1) % 3, eprev = (it + 2) % 3;
+          HL.h.p.parity = cur;
+          HL.h.p.src = src[it];
+          HL.h.p.cor = it > 0 ? src[it - 1] : 0.0f;
+          CK(half_scales(h.Mx + cur * sz, h.Mx + prv * sz, h.E + enew * sz, sz, HL.h.p.one.src_z,
+                         fabsf(HL.h.p.src) + fabsf(HL.h.p.cor), cs));
+          HL.h.out_hi = h.hi[prv];
+          HL.h.out_lo = h.lo[prv];
+          HL.h.e_cur = h.E + ecur * sz;
+          HL.h.e_prev = h.E + eprev * sz;
+          HL.h.e_new = h.E + enew * sz;
+          HL.h.m_new = h.Mx + prv * sz;
+          HL.m = B.h_hmaps[i].m[cur];
+          CK(propagate_half_launch(HL, ext, cs));
+          B.launches += 2;
+        }
+        continue;
+      }
       const ShotMaps &m = B.h_maps[i];
       P.one = B.s_desc[i];
       P.nitems = B.s_nitems[i];
@@ -2125,10 +2169,19 @@ extern "C" int FLETCHER_BatchRun(const float *src, int max_steps, int use_graph,
   if (per_sm < 1)
     return fail(FLETCHER_ERR_CUDA, "tile shape (%d rows, %d stages) fits no CTA on an SM", B.sealed_rows, B.stages);
   B.ctas = B.num_sms * per_sm;
-  const int nchains = batch_half() ? 0 : (B.chains < 0 ? batch_auto_chains(steps) : B.chains);
+  const int nchains = B.chains < 0 ? batch_auto_chains(steps) : B.chains;
   B.last_chains = nchains;
   const bool chains = nchains > 0;
-  if (chains ? batch_single_plans(B.ctas) : (!batch_half() && batch_plan(B.ctas))) return g_last_err;
+  int plan_ctas = B.ctas;
+  if (chains && batch_half()) {
+    // The single-shot 16-bit kernel: its own attributes and residency.
+    const bool ext = B.form == FLETCHER_FORM_FP16X;
+    if (propagate_half_prepare(B.sealed_rows, B.stages, ext, false) != cudaSuccess)
+      return fail(FLETCHER_ERR_CUDA, "kernel attribute set-up failed");
+    plan_ctas = B.num_sms * propagate_half_ctas_per_sm(B.sealed_rows, B.stages, ext, false);
+    if (plan_ctas < 1) return fail(FLETCHER_ERR_CUDA, "tile shape fits no single-shot CTA on an SM");
+  }
+  if (chains ? batch_single_plans(plan_ctas) : (!batch_half() && batch_plan(B.ctas))) return g_last_err;
   auto issue = [&]() { return chains ? batch_issue_chains(nchains, steps, src) : batch_issue(0, steps, src); };
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));

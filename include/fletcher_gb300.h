@@ -317,22 +317,23 @@ int FLETCHER_BatchCreate(int bord, float dx, float dy, float dz, float dt);
 int FLETCHER_BatchAddShot(int sx, int sy, int sz, const float *model, long iSource, int nsteps);
 /* Tile shape for the next FLETCHER_BatchRun (0 = default). */
 int FLETCHER_BatchSetTileConfig(int tile_rows, int stages);
-/* Schedule of an FP32 batch's run, after FLETCHER_BatchCreate.
+/* Schedule of a batch's run, after FLETCHER_BatchCreate.
  * chains = -1 (default): one chain when most of the batch's work (updated
  *   cells x steps) is in shots of at least 2.1 M updated cells, which fill
  *   the GPU on their own, else the persistent launch (measured on GB300: 48
  *   shots of 168^3-392^3 ran 7% faster on one chain than on the persistent
  *   launch; 48 shots of 56^3 and 32 of 80^3 ran 6-7% slower).
  * chains = 0: one persistent launch per time step advances every running
- *   shot (the shots' single-shot plans stacked per CTA).
+ *   shot (FP32: the shots' single-shot plans stacked per CTA; 16-bit forms:
+ *   the plane-scale launch of every running shot first).
  * chains = 1 .. 8: every step of a shot is its own single-shot launch; the
  *   shots are dealt, largest work first, over `chains` concurrent streams,
  *   each running its shots one after another (one graph when captured).
  *   A launch waits on no other kernel, so kernels of different chains
  *   share the GPU where one leaves SMs idle, and each chain works on one
- *   shot's memory at a time.
- * Results are bit-identical in every schedule.  16-bit batches always use
- * the persistent launch. */
+ *   shot's memory at a time.  In the 16-bit forms each step is the
+ *   single-shot pair of launches (the new planes' scales, then the step).
+ * Results are bit-identical in every schedule. */
 int FLETCHER_BatchSetChains(int chains);
 /* The schedule of the last FLETCHER_BatchRun: 0 (persistent launch) or the
  * number of chains. */

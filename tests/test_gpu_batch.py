@@ -217,3 +217,28 @@ def test_default_schedule_follows_shot_size():
         assert chains == want
         for i, (p, m) in enumerate(zip(shots, models)):
             assert np.array_equal(got[i], single(p, m)[0]), (want, i)
+
+
+@pytest.mark.parametrize("form", ["fp16", "fp16x"])
+@pytest.mark.parametrize("chains", [1, 2])
+def test_half_chain_schedule_matches_single_shot_runs(form, chains):
+    """The chain schedule in the 16-bit forms: each step of a shot is the
+    single-shot pair of launches (plane scales, step) on its chain's stream;
+    every shot equals its single-shot run in that form, graph or not."""
+    shots = SHOTS + [Problem("h3", 70, 60, 150, absorb=5, dt=0.0006, steps=13, fcut=45.0, kind="layered", layers=4,
+                             seed=34, source=(35, 30, 70))]
+    models = [p.model() for p in shots]
+    for use_graph in (True, False):
+        batch = Batch(form=form, chains=chains)
+        for p, m in zip(shots, models):
+            batch.add(p, m)
+        batch.run(use_graph=use_graph)
+        got = [[batch.field(i, k) for k in range(4)] for i in range(len(shots))]
+        info = batch.info()
+        batch.close()
+        assert info["chains"] == chains
+        for i, (p, m) in enumerate(zip(shots, models)):
+            ref = single(p, m, form)
+            assert np.abs(ref[0]).max() > 0.0
+            for k in range(4):
+                assert np.array_equal(got[i][k], ref[k]), (form, chains, use_graph, i, k)
