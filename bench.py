@@ -295,11 +295,18 @@ def run_gb300(args, ws, rank, local, group):
     e2e = e2e_wall = parity = e2e_clk = None
     KE = args.e2e_steps or prob.steps  # the workload's own step count (1000 at C1)
     if not args.no_e2e:
-        # The initial fields are written (zeroed) by the caller before the
-        # call, as the reference's main() does (original/main.c:257-258); pages
-        # never written would make locking them for the copies allocate them.
-        f = np.empty((4, prob.n), np.float32)
-        f.fill(0.0)
+        # The caller's host arrays -- the six model arrays and the four
+        # fields, zeroed as the reference's main() does (original/main.c:
+        # 257-258) -- live in page-locked memory it allocated beforehand, so
+        # every copy in the call runs from pinned host memory at the link's
+        # rate (the library copies page-locked arrays as they are and locks
+        # pageable ones for their copies, whose speed then depends on how the
+        # system backs their pages).
+        pin_f = torch.zeros((4, prob.n), dtype=torch.float32, pin_memory=True)
+        pin_m = torch.empty((6, prob.n), dtype=torch.float32, pin_memory=True)
+        f = pin_f.numpy()
+        model_e2e = pin_m.numpy()
+        model_e2e[...] = model
         from fletcher_petrobras_gb300.driver import FORMS
 
         from fletcher_petrobras_gb300.driver import COEF_LAYOUTS
@@ -307,12 +314,21 @@ def run_gb300(args, ws, rank, local, group):
         lib.FLETCHER_SetForm(FORMS[form])
         lib.FLETCHER_SetCoefLayout(COEF_LAYOUTS[args.coef_layout])
         lib.FLETCHER_SetStream(None)  # the library's own stream, as a plain C caller has it
+        # Untimed warm-up: a 2-step call on the same buffers (their first
+        # transfers set up the mappings of freshly locked memory), then the
+        # fields are zeroed again.
+        rc = lib.FLETCHER_Model(2, prob.i_source, prob.fcut, 0.0, prob.sx, prob.sy, prob.sz, prob.bord, prob.dx,
+                                prob.dy, prob.dz, prob.dt, *[fptr(f[k]) for k in range(4)],
+                                *[fptr(model_e2e[k]) for k in range(6)], stats)
+        if rc:
+            raise RuntimeError("FLETCHER_Model failed: " + lib.FLETCHER_GetLastErrorString().decode())
+        f[...] = 0.0
         group.barrier()
         e2e_clocks = ClockSampler(local)
         e2e_clocks.start()
         rc = lib.FLETCHER_Model(KE, prob.i_source, prob.fcut, 0.01, prob.sx, prob.sy, prob.sz, prob.bord, prob.dx,
                                 prob.dy, prob.dz, prob.dt, *[fptr(f[k]) for k in range(4)],
-                                *[fptr(model[k]) for k in range(6)], stats)
+                                *[fptr(model_e2e[k]) for k in range(6)], stats)
         e2e_clk = e2e_clocks.stop()
         if rc:
             raise RuntimeError("FLETCHER_Model failed: " + lib.FLETCHER_GetLastErrorString().decode())
@@ -325,7 +341,7 @@ def run_gb300(args, ws, rank, local, group):
         e2e_wall = group.reduce(stats[2], "max")
         e2e = ws * cells * KE / e2e_wall / 1e6
         parity = reference_parity(prob, KE, form, f[1], f[3])  # FLETCHER_Model leaves the final p, q in pc, qc
-        del f
+        del f, model_e2e, pin_f, pin_m
 
     # The other storage forms on the same workload (fewer steps).
     forms = {}
@@ -391,7 +407,8 @@ def run_gb300(args, ws, rank, local, group):
                 "clocks": e2e_clk,
                 "what": f"FLETCHER_Model via the C ABI, the workload's {KE} steps: DRIVER_Initialize (H2D of 6 "
                         "model + 4 field arrays, FP64 coefficient precompute) + per step (InsertSource, Propagate) "
-                        "+ D2H snapshot of p every 0.01 s simulated + final D2H of p,q"},
+                        "+ D2H snapshot of p every 0.01 s simulated + final D2H of p,q; the caller's host arrays "
+                        "in page-locked memory allocated before the call; one untimed 2-step call before"},
         "gpu_launches": launches,
         "clocks": clk,
     }

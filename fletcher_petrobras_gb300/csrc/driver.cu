@@ -166,12 +166,17 @@ ResidentView resident_view() {
 
 namespace {
 
+// A failed call is recorded in the library's status; the runtime's own
+// last-error state is cleared (for the errors that are not sticky), so a
+// later launch check does not report it again.
 #define CK(call)                                                                                   \
   do {                                                                                             \
     cudaError_t e_ = (call);                                                                       \
-    if (e_ != cudaSuccess)                                                                         \
+    if (e_ != cudaSuccess) {                                                                       \
+      cudaGetLastError();                                                                          \
       return fail(e_ == cudaErrorMemoryAllocation ? FLETCHER_ERR_NOMEM : FLETCHER_ERR_CUDA,       \
                   "%s failed at %s:%d: %s", #call, __FILE__, __LINE__, cudaGetErrorString(e_));   \
+    }                                                                                              \
   } while (0)
 
 // Device allocation through the fault-injection countdown.

@@ -150,3 +150,31 @@ def test_consecutive_snapshots_each_hold_their_step(tmp_path, monkeypatch):
     x = open(os.path.join(tmp_path, "mid.rsf@"), "rb").read()
     y = open(os.path.join(tmp_path, "ref.rsf@"), "rb").read()
     assert len(x) == 4 * (box[1] - box[0] + 1) * (box[3] - box[2] + 1) and x == y
+
+
+def test_model_loop_with_page_locked_caller_arrays():
+    """The caller's arrays already page-locked (cudaHostAlloc'd by torch):
+    the library's own locking of them fails, is not an error, and leaves no
+    CUDA error state behind; the run equals one on ordinary arrays."""
+    import ctypes as C
+
+    import torch
+
+    p = PROB
+    m = p.model()
+    outs = []
+    for pinned in (False, True):
+        if pinned:
+            tf = torch.zeros((4, p.n), dtype=torch.float32, pin_memory=True)
+            tm = torch.empty((6, p.n), dtype=torch.float32, pin_memory=True)
+            f, mm = tf.numpy(), tm.numpy()
+            mm[...] = m
+        else:
+            f, mm = np.zeros((4, p.n), np.float32), m
+        lib = Propagator().lib
+        stats = (C.c_double * 5)()
+        rc = lib.FLETCHER_Model(p.steps, p.i_source, p.fcut, 0.003, p.sx, p.sy, p.sz, p.bord, p.dx, p.dy, p.dz, p.dt,
+                                *[fptr(f[k]) for k in range(4)], *[fptr(mm[k]) for k in range(6)], stats)
+        assert rc == 0, lib.FLETCHER_GetLastErrorString()
+        outs.append(f.copy())
+    assert np.array_equal(outs[0], outs[1])
