@@ -128,6 +128,8 @@ def test_argument_errors_are_reported_not_fatal(lib):
     lib.FLETCHER_ClearError()
     ph = (ctypes.c_double * 5)()
     assert lib.FLETCHER_InitPhases(ph) == 0
+    assert lib.FLETCHER_DebugPoisonPadding(0.0) == 1  # not initialised
+    lib.FLETCHER_ClearError()
 
 
 @pytest.mark.skipif(reference_dir() is None, reason="reference sources absent (FLETCHER_REF_DIR or staged copy)")
