@@ -1901,8 +1901,9 @@ int batch_issue(int it0, int it1, const float *src) {
 }
 
 // The chain schedule: steps [0, steps) of every shot as single-shot
-// launches, the shots dealt (largest work first, to the least loaded chain)
-// over B.chains streams forked from and joined back into the library's
+// launches, the shots dealt (longest run first, each to the chain with the
+// least work so far) over B.chains streams forked from and joined back into
+// the library's
 // stream, so the whole run is one graph when captured.  A launch waits on
 // no other kernel, so kernels of different chains may share the GPU.
 int batch_issue_chains(int chains, int steps, const float *src) {

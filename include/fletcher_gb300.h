@@ -327,7 +327,8 @@ int FLETCHER_BatchSetTileConfig(int tile_rows, int stages);
  *   shot (FP32: the shots' single-shot plans stacked per CTA; 16-bit forms:
  *   the plane-scale launch of every running shot first).
  * chains = 1 .. 8: every step of a shot is its own single-shot launch; the
- *   shots are dealt, largest work first, over `chains` concurrent streams,
+ *   shots are dealt, longest run first, each to the stream with the least
+ *   work so far, over `chains` concurrent streams,
  *   each running its shots one after another (one graph when captured).
  *   A launch waits on no other kernel, so kernels of different chains
  *   share the GPU where one leaves SMs idle, and each chain works on one
